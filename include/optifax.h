@@ -1,0 +1,144 @@
+/*
+ * optifax.h -- C ABI of the GB300 (sm_103a) chi(2) crystal-pass propagator.
+ *
+ * Drop-in for OptiFax's crystal-pass solver boundary.  In the reference the
+ * boundary is the MATLAB function handle OpticalSim.Solver
+ * (toolbox/lib/classes/OpticalSim.m:20,98-100,237-252) resolving to the MEX
+ * gateway mexFunction (toolbox/lib/MEXlib/src/OPO_mex_BATCH.cpp:19-141) which
+ * calls the host driver OPO_TEST_CUDA
+ * (toolbox/lib/MEXlib/src/OPO_CUDA_BATCH_XTAL.cu:373-525,
+ *  prototype toolbox/lib/MEXlib/src/OPO_BATCH_HEADER.hpp:8-28).
+ *
+ * All array arguments are DEVICE pointers owned by the caller; complex arrays
+ * are interleaved (re, im) single precision, i.e. MATLAB complex single
+ * gpuArrays / CUDA float2.  Every call is ordered on the given CUDA stream
+ * (NULL = legacy default stream) and returns before the work completes.
+ * Functions return OPTIFAX_OK or an optifax_status code; they never abort.
+ * A handle may be used by one host thread at a time.
+ */
+#ifndef OPTIFAX_H
+#define OPTIFAX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct optifax_context* optifax_handle;
+
+typedef enum {
+    OPTIFAX_OK = 0,
+    OPTIFAX_ERR_INVALID_ARGUMENT = 1,
+    OPTIFAX_ERR_UNSUPPORTED = 2,
+    OPTIFAX_ERR_CUDA = 3,
+    OPTIFAX_ERR_NO_MEMORY = 4,
+    OPTIFAX_ERR_NULL_HANDLE = 5
+} optifax_status;
+
+/* Integration scheme of the nonlinear sub-step. */
+typedef enum {
+    OPTIFAX_HEUN = 0,   /* OPO_CUDA_BATCH_XTAL.cu:432-506 (Euler + Heun, +1 growth) */
+    OPTIFAX_RK23 = 1    /* ode23/OPO_CUDA_ODE23.cu:428-538 (Bogacki-Shampine, x2 growth) */
+} optifax_method;
+
+/* Reference source variant whose conventions are reproduced. */
+typedef enum {
+    OPTIFAX_VARIANT_BATCH_XTAL = 0, /* shifted time, sech^2 absorber, ceil chunk count + k<Nsteps guard, G is S x B */
+    OPTIFAX_VARIANT_BATCH_OP = 1,   /* as XTAL with one G shared by all pulses (OPO_CUDA_BATCH_OP.cu:221) */
+    OPTIFAX_VARIANT_NO_BC = 2,      /* unshifted time, no absorber, truncated chunk count (OPO_CUDA_NO_BC.cu) */
+    OPTIFAX_VARIANT_HARD_BC = 3,    /* unshifted time, hard absorber (OPO_CUDA_HARD_BC.cu:118-129) */
+    OPTIFAX_VARIANT_ODE23 = 4       /* unshifted time, sech^2 absorber, truncated chunks, shared G (OPO_CUDA_ODE23.cu) */
+} optifax_variant;
+
+/* Per-pulse status bits returned in optifax_pulse_stats.status. */
+#define OPTIFAX_PULSE_NAN           0x1  /* a non-finite field value was produced */
+#define OPTIFAX_PULSE_ATTEMPT_LIMIT 0x2  /* the step-attempt safety limit was reached */
+
+typedef struct {
+    int32_t attempts;       /* step attempts (accepted + rejected) */
+    int32_t accepted;
+    int32_t rejected;
+    int32_t status;         /* OPTIFAX_PULSE_* bits */
+    int64_t z_steps;        /* sum of stepmod over accepted steps (distance / h) */
+    float k_final;          /* final value of the reference's step counter k */
+    float stepmod_final;
+    int32_t n_chunks;
+    int32_t reserved[3];
+} optifax_pulse_stats;
+
+/* One crystal pass of one pulse (all pointers are device pointers). */
+typedef struct {
+    int32_t n_points;        /* N: power of two, 512 .. 65536 */
+    int32_t n_steps;         /* S = floor(L / h) */
+    const void* E_in;        /* N complex: fftshifted temporal field (t = 0 at index 0) */
+    void* A_out;             /* N complex output field (may alias E_in) */
+    const float* alpha;      /* N: per-step power transmission, FFT order (TStepShift) */
+    const float* beta;       /* N: relative phase per step h, FFT order (hBshift) */
+    const float* G;          /* S: QPM-signed coupling G33 per z-sample */
+    void* Ap;                /* optional: spectral snapshots, N x n_chunks complex, reference layout */
+    float* stepmods;         /* optional: S floats, stepmods[k] = stepmod of the accepted step at k */
+    int32_t* trace;          /* optional: 3 ints per attempt (k, stepmod, flags) */
+    const int32_t* forced;   /* optional: per-attempt decisions to replay (bit0 >maxErr, bit1 >minErr) */
+    int32_t trace_cap;
+    int32_t n_forced;
+    float w0;                /* reference angular frequency (single, as the MEX casts it) */
+    float h;                 /* step size [m] (single) */
+    double bdiffw0;          /* beta0(w0) - beta1(w0) w0 */
+    double dt;               /* time step [s] */
+    float max_err;           /* percent */
+    float min_err;           /* percent */
+    float sel;               /* steps per progress chunk */
+    int32_t stepmods_limit;  /* stepmods recorded for k < limit (0: the variant's own rule) */
+} optifax_pulse;
+
+/* Create / destroy a context on a CUDA device.  The context owns the twiddle
+ * tables and the pulse-descriptor staging buffers (device workspace). */
+int optifax_create(optifax_handle* out, int device);
+int optifax_destroy(optifax_handle h);
+const char* optifax_status_string(int status);
+/* Human-readable detail of the last failure on this handle. */
+const char* optifax_last_error(optifax_handle h);
+
+/*
+ * The MEX-shaped entry: the 14 solver inputs of OPO_mex_BATCH.cpp:42-56 and
+ * its 3 outputs (:120-122), replacing mexFunction + OPO_TEST_CUDA.
+ *   E        prhs[0]  N x B complex, fftshifted time
+ *   alpha_w  prhs[1]  N   (TStepShift)
+ *   G        prhs[2]  S (BATCH_OP/ODE23 variants) or S x B (BATCH_XTAL)
+ *   w0       prhs[3], bdiffw0 prhs[4], h prhs[5], n_steps prhs[6], dt prhs[7]
+ *   beta_op  prhs[8]  N   (hBshift; N = numel)
+ *   max_pct_err prhs[9], min_pct_err prhs[10], sel prhs[11]
+ *   Ap_in    prhs[12] N x ap_chunks x B complex
+ *   stepmods_in prhs[13] S
+ * Outputs: A_out (plhs[0], N x B), Ap_out (plhs[1]), stepmods_out (plhs[2]);
+ * the outputs may alias the inputs.  As in the reference, all pulses of the
+ * batch share one adaptive step schedule (error flags are OR-ed over the
+ * batch): for n_pulses > 1 the batch runs as one cooperative launch.
+ */
+int optifax_opo_mex_batch(optifax_handle h,
+                          const void* E, const float* alpha_w, const float* G,
+                          float w0, double bdiffw0, float step_h, int32_t n_steps, double dt,
+                          const float* beta_op, float max_pct_err, float min_pct_err, float sel,
+                          const void* Ap_in, const float* stepmods_in,
+                          int32_t n_points, int32_t n_pulses, int32_t ap_chunks, int32_t variant,
+                          void* A_out, void* Ap_out, float* stepmods_out, void* stream);
+
+/*
+ * Batched crystal passes with per-pulse grids and step schedules: each pulse
+ * carries its own N, S, crystal and tolerances, and adapts its own step
+ * (unlike the reference, whose batch shares one schedule).  `pulses` is a
+ * HOST array of n_pulses descriptors holding device pointers.  stats
+ * (optional) is a DEVICE array of n_pulses entries.  cta_points selects the
+ * points held per CTA (512..4096, 0 = automatic); a pulse of N points runs on
+ * a cluster of N / cta_points CTAs.
+ */
+int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
+                      int32_t method, int32_t variant, int32_t cta_points,
+                      optifax_pulse_stats* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OPTIFAX_H */

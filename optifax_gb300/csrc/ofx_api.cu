@@ -1,0 +1,378 @@
+// ofx_api.cu -- C ABI (include/optifax.h): context, twiddle tables,
+// descriptor staging, validation and launch of the crystal-pass kernels.
+//
+// Replaces the MEX gateway mexFunction (toolbox/lib/MEXlib/src/OPO_mex_BATCH.cpp:19-141)
+// and the host driver OPO_TEST_CUDA (OPO_CUDA_BATCH_XTAL.cu:373-525,
+// ode23/OPO_CUDA_ODE23.cu:375-557): instead of ~10 launches, two cuFFT calls
+// and two device synchronisations per step, one launch runs every step of
+// every pulse.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ofx_kernels.cuh"
+#include "../../include/optifax.h"
+
+using namespace ofx;
+
+struct optifax_context {
+    int device = 0;
+    std::map<int, Twiddle*> tw;          // n -> n/2 entries, W_n^e
+    PulseDev* d_desc = nullptr;
+    size_t desc_cap = 0;
+    int* d_grid_flags = nullptr;
+    std::string last_error;
+};
+
+namespace {
+
+__global__ void twiddle_kernel(Twiddle* out, int n) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n / 2) return;
+    double s, c;
+    sincospi(-2.0 * (double)e / (double)n, &s, &c);
+    float cf = (float)c, sf = (float)s;
+    double m2 = (double)cf * (double)cf + (double)sf * (double)sf;
+    Twiddle w;
+    w.c = cf; w.s = sf; w.d = (float)(1.0 / m2 - 1.0); w.pad = 0.f;
+    out[e] = w;
+}
+
+int fail(optifax_context* h, int code, const std::string& msg) {
+    if (h) h->last_error = msg;
+    return code;
+}
+
+int cuda_fail(optifax_context* h, cudaError_t e, const char* what) {
+    return fail(h, OPTIFAX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+const Twiddle* get_twiddles(optifax_context* h, int n, cudaStream_t st, int* rc) {
+    auto it = h->tw.find(n);
+    if (it != h->tw.end()) return it->second;
+    Twiddle* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(Twiddle) * (size_t)(n / 2));
+    if (e != cudaSuccess) { *rc = cuda_fail(h, e, "cudaMalloc(twiddles)"); return nullptr; }
+    twiddle_kernel<<<(n / 2 + 255) / 256, 256, 0, st>>>(d, n);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) { cudaFree(d); *rc = cuda_fail(h, e, "twiddle_kernel"); return nullptr; }
+    // tables are shared by every stream of the context: finish building them now
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { cudaFree(d); *rc = cuda_fail(h, e, "twiddle_kernel sync"); return nullptr; }
+    h->tw[n] = d;
+    return d;
+}
+
+uint64_t turns_fixed(long double radians) {
+    long double tw = radians / (2.0L * 3.14159265358979323846264338327950288L);
+    tw -= floorl(tw);                        // [0, 1)
+    long double x = tw * 18446744073709551616.0L;
+    if (x >= 18446744073709551615.0L) return 0;
+    return (uint64_t)x;
+}
+
+const std::vector<KernelEntry>& kernel_table() {
+    static const std::vector<KernelEntry> tbl = [] {
+        std::vector<KernelEntry> v;
+        register_kernels_heun_large(v);
+        register_kernels_heun_small(v);
+        register_kernels_rk23(v);
+        return v;
+    }();
+    return tbl;
+}
+
+const KernelEntry* find_kernel(int M, int C, int method) {
+    for (const auto& k : kernel_table())
+        if (k.M == M && k.C == C && k.method == method) return &k;
+    return nullptr;
+}
+
+struct VariantCfg { int time_mode, abc_mode, guard, g_per_pulse, stepmods_rule; };
+
+bool variant_cfg(int variant, VariantCfg* v) {
+    switch (variant) {
+        case OPTIFAX_VARIANT_BATCH_XTAL: *v = {TIME_SHIFTED, ABC_SOFT, 1, 1, 128}; return true;
+        case OPTIFAX_VARIANT_BATCH_OP:   *v = {TIME_SHIFTED, ABC_SOFT, 1, 0, 128}; return true;
+        case OPTIFAX_VARIANT_NO_BC:      *v = {TIME_UNSHIFTED, ABC_NONE, 0, 0, 128}; return true;
+        case OPTIFAX_VARIANT_HARD_BC:    *v = {TIME_UNSHIFTED, ABC_HARD, 0, 0, 128}; return true;
+        case OPTIFAX_VARIANT_ODE23:      *v = {TIME_UNSHIFTED, ABC_SOFT, 0, 0, 256}; return true;
+        default: return false;
+    }
+}
+
+int stepmods_limit_for(int N, int rule) {
+    // Dispersion_kernel records stepmods[k] in the thread with gx == k, gx in
+    // [0, gridDim.x * blockDim.x): ceil(N/128)*128 (BATCH kernels) or
+    // (N/256)*256 (ODE23, which launches N/256 blocks).
+    return rule == 128 ? ((N + 127) / 128) * 128 : (N / 256) * 256;
+}
+
+int n_chunks_for(int S, float sel, int guard) {
+    int nc = (int)((float)S / sel);
+    if (guard && (float)nc * sel < (float)S) nc += 1;
+    return nc;
+}
+
+int choose_M(int N, int cta_points) {
+    if (cta_points > 0) return cta_points;
+    return N <= 4096 ? N : 4096;
+}
+
+// Build descriptors of one launch group and launch it.
+int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, int C, int method,
+                 const VariantCfg& vc, bool shared, cudaStream_t st) {
+    const KernelEntry* ke = find_kernel(M, C, method);
+    if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
+                         "no kernel for cta_points=" + std::to_string(M) + " cluster=" + std::to_string(C));
+    int rc = OPTIFAX_OK;
+    const Twiddle* twM = get_twiddles(h, M, st, &rc);
+    if (!twM) return rc;
+    const Twiddle* twN = (C > 1) ? get_twiddles(h, M * C, st, &rc) : twM;
+    if (!twN) return rc;
+    size_t nb = descs.size() * sizeof(PulseDev);
+    if (nb > h->desc_cap) {
+        if (h->d_desc) { cudaStreamSynchronize(st); cudaFree(h->d_desc); h->d_desc = nullptr; }
+        size_t cap = nb < 4096 ? 4096 : nb * 2;
+        cudaError_t e = cudaMalloc(&h->d_desc, cap);
+        if (e != cudaSuccess) { h->desc_cap = 0; return cuda_fail(h, e, "cudaMalloc(descriptors)"); }
+        h->desc_cap = cap;
+    }
+    cudaError_t e = cudaMemcpyAsync(h->d_desc, descs.data(), nb, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(descriptors)");
+    if (shared) {
+        e = cudaMemsetAsync(h->d_grid_flags, 0, 4 * sizeof(int), st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync(grid flags)");
+    }
+    e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ke->smem);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(smem)");
+    if (C > 8) {
+        e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(cluster 16)");
+    }
+    KernelCfg cfg;
+    cfg.time_mode = vc.time_mode;
+    cfg.abc_mode = vc.abc_mode;
+    cfg.guard = vc.guard;
+    cfg.shared_sched = shared ? 1 : 0;
+    cfg.max_attempts_mul = 64;
+    cfg.grid_flags = h->d_grid_flags;
+
+    cudaLaunchConfig_t lc;
+    memset(&lc, 0, sizeof(lc));
+    lc.gridDim = dim3((unsigned)(descs.size() * C), 1, 1);
+    lc.blockDim = dim3(M / 16, 1, 1);
+    lc.dynamicSmemBytes = ke->smem;
+    lc.stream = st;
+    cudaLaunchAttribute attrs[2];
+    int na = 0;
+    attrs[na].id = cudaLaunchAttributeClusterDimension;
+    attrs[na].val.clusterDim.x = C; attrs[na].val.clusterDim.y = 1; attrs[na].val.clusterDim.z = 1;
+    ++na;
+    if (shared) {
+        attrs[na].id = cudaLaunchAttributeCooperative;
+        attrs[na].val.cooperative = 1;
+        ++na;
+    }
+    lc.attrs = attrs;
+    lc.numAttrs = na;
+    const PulseDev* dd = h->d_desc;
+    e = cudaLaunchKernelEx(&lc, ke->fn, dd, twM, twN, cfg);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaLaunchKernelEx(pass_kernel)");
+    return OPTIFAX_OK;
+}
+
+bool is_pow2(long long x) { return x > 0 && (x & (x - 1)) == 0; }
+
+int fill_desc(optifax_context* h, const optifax_pulse& in, const VariantCfg& vc, PulseDev* d,
+              optifax_pulse_stats* stats) {
+    if (!is_pow2(in.n_points) || in.n_points < 512 || in.n_points > 65536)
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_points must be a power of two in [512, 65536]");
+    if (in.n_steps < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_steps must be >= 1");
+    if (!(in.sel >= 1.0f)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "sel must be >= 1");
+    if (!(in.h > 0.0f) || !(in.dt > 0.0) || !(in.w0 > 0.0f))
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "h, dt and w0 must be positive");
+    if (!in.E_in || !in.A_out || !in.alpha || !in.beta || !in.G)
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "E_in, A_out, alpha, beta and G are required");
+    if ((in.trace && in.trace_cap < 0) || (in.forced && in.n_forced < 0))
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "negative trace/forced length");
+    const long long n_att_bound = 64LL * (in.n_steps + 16) + 64;
+    if (n_att_bound > 0x7fffffffLL || (long long)in.n_steps * 4 > (1LL << 24))
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_steps too large (4*S must stay below 2^24)");
+    memset(d, 0, sizeof(*d));
+    d->E_in = (const float2*)in.E_in;
+    d->A_out = (float2*)in.A_out;
+    d->alpha = in.alpha;
+    d->beta = in.beta;
+    d->G = in.G;
+    d->Ap = (float2*)in.Ap;
+    d->stepmods = in.stepmods;
+    d->trace = in.trace;
+    d->forced = in.forced;
+    d->stats = stats;
+    d->bdiffw0 = in.bdiffw0;
+    d->dt = in.dt;
+    d->tau_theta = turns_fixed((long double)(double)in.w0 * (long double)in.dt);
+    d->tau_z4 = turns_fixed((long double)in.bdiffw0 * (long double)(double)in.h / 4.0L);
+    d->w0 = in.w0;
+    d->h = in.h;
+    d->max_err = in.max_err;
+    d->min_err = in.min_err;
+    d->sel = in.sel;
+    float invdt2 = (float)(1.0 / (2.0 * in.dt));
+    d->c_shock = invdt2 / in.w0;
+    d->N = in.n_points;
+    d->S = in.n_steps;
+    d->nchunks = n_chunks_for(in.n_steps, in.sel, vc.guard);
+    d->stepmods_limit = in.stepmods_limit > 0 ? in.stepmods_limit : stepmods_limit_for(in.n_points, vc.stepmods_rule);
+    d->trace_cap = in.trace ? in.trace_cap : 0;
+    d->n_forced = in.forced ? in.n_forced : 0;
+    return OPTIFAX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int optifax_create(optifax_handle* out, int device) {
+    if (!out) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n <= 0) return OPTIFAX_ERR_CUDA;
+    if (device < 0 || device >= n) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    optifax_context* h = new (std::nothrow) optifax_context();
+    if (!h) return OPTIFAX_ERR_NO_MEMORY;
+    h->device = device;
+    e = cudaMalloc(&h->d_grid_flags, 4 * sizeof(int));
+    if (e != cudaSuccess) { delete h; return OPTIFAX_ERR_CUDA; }
+    *out = h;
+    return OPTIFAX_OK;
+}
+
+int optifax_destroy(optifax_handle h) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    cudaSetDevice(h->device);
+    cudaDeviceSynchronize();
+    for (auto& kv : h->tw) cudaFree(kv.second);
+    if (h->d_desc) cudaFree(h->d_desc);
+    if (h->d_grid_flags) cudaFree(h->d_grid_flags);
+    delete h;
+    return OPTIFAX_OK;
+}
+
+const char* optifax_status_string(int status) {
+    switch (status) {
+        case OPTIFAX_OK: return "ok";
+        case OPTIFAX_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case OPTIFAX_ERR_UNSUPPORTED: return "unsupported configuration";
+        case OPTIFAX_ERR_CUDA: return "CUDA error";
+        case OPTIFAX_ERR_NO_MEMORY: return "out of memory";
+        case OPTIFAX_ERR_NULL_HANDLE: return "null handle";
+        default: return "unknown status";
+    }
+}
+
+const char* optifax_last_error(optifax_handle h) {
+    return h ? h->last_error.c_str() : "null handle";
+}
+
+int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
+                      int32_t method, int32_t variant, int32_t cta_points,
+                      optifax_pulse_stats* stats, void* stream) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!pulses || n_pulses < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "no pulses");
+    if (method != OPTIFAX_HEUN && method != OPTIFAX_RK23)
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown method");
+    VariantCfg vc;
+    if (!variant_cfg(variant, &vc)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown variant");
+    if (cta_points != 0 && (!is_pow2(cta_points) || cta_points < 512 || cta_points > 4096))
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "cta_points must be 0 or a power of two in [512, 4096]");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    cudaStream_t st = (cudaStream_t)stream;
+    // group pulses by (M, C)
+    std::map<std::pair<int, int>, std::vector<PulseDev>> groups;
+    for (int i = 0; i < n_pulses; ++i) {
+        PulseDev d;
+        int rc = fill_desc(h, pulses[i], vc, &d, stats ? stats + i : nullptr);
+        if (rc) return rc;
+        int M = choose_M(pulses[i].n_points, cta_points);
+        if (M > pulses[i].n_points) M = pulses[i].n_points;
+        int C = pulses[i].n_points / M;
+        if (C > 16) return fail(h, OPTIFAX_ERR_UNSUPPORTED, "n_points / cta_points exceeds 16");
+        groups[{M, C}].push_back(d);
+    }
+    // One launch per (M, C) group; a group's descriptors are staged in the
+    // context buffer, so groups are launched one after another on the stream.
+    for (auto& g : groups) {
+        int rc = launch_group(h, g.second, g.first.first, g.first.second, method, vc, false, st);
+        if (rc) return rc;
+    }
+    return OPTIFAX_OK;
+}
+
+int optifax_opo_mex_batch(optifax_handle h,
+                          const void* E, const float* alpha_w, const float* G,
+                          float w0, double bdiffw0, float step_h, int32_t n_steps, double dt,
+                          const float* beta_op, float max_pct_err, float min_pct_err, float sel,
+                          const void* Ap_in, const float* stepmods_in,
+                          int32_t n_points, int32_t n_pulses, int32_t ap_chunks, int32_t variant,
+                          void* A_out, void* Ap_out, float* stepmods_out, void* stream) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    VariantCfg vc;
+    if (!variant_cfg(variant, &vc)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown variant");
+    if (n_pulses < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_pulses must be >= 1");
+    if (!Ap_out || !stepmods_out) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "Ap_out and stepmods_out are required");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    cudaStream_t st = (cudaStream_t)stream;
+    int method = (variant == OPTIFAX_VARIANT_ODE23) ? OPTIFAX_RK23 : OPTIFAX_HEUN;
+    int nchunks = n_chunks_for(n_steps, sel, vc.guard);
+    if (nchunks > ap_chunks)
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "Ap has fewer chunks than ceil(n_steps/sel)");
+    size_t n = (size_t)n_points;
+    // outputs start as copies of the inputs (mxGPUCopyFromMxArray, OPO_mex_BATCH.cpp:55-56)
+    if (Ap_in && Ap_in != Ap_out) {
+        e = cudaMemcpyAsync(Ap_out, Ap_in, sizeof(float2) * n * (size_t)ap_chunks * (size_t)n_pulses,
+                            cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "copy Ap");
+    }
+    if (stepmods_in && stepmods_in != stepmods_out) {
+        e = cudaMemcpyAsync(stepmods_out, stepmods_in, sizeof(float) * (size_t)n_steps,
+                            cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "copy stepmods");
+    }
+    std::vector<PulseDev> descs((size_t)n_pulses);
+    for (int b = 0; b < n_pulses; ++b) {
+        optifax_pulse p;
+        memset(&p, 0, sizeof(p));
+        p.n_points = n_points;
+        p.n_steps = n_steps;
+        p.E_in = (const float2*)E + n * b;
+        p.A_out = (float2*)A_out + n * b;
+        p.alpha = alpha_w;
+        p.beta = beta_op;
+        p.G = vc.g_per_pulse ? G + (size_t)n_steps * b : G;
+        // reference layout: (b * Nchunks + chunk) * N + i (OPO_CUDA_BATCH_XTAL.cu:302)
+        p.Ap = (float2*)Ap_out + (size_t)b * (size_t)nchunks * n;
+        p.stepmods = stepmods_out;
+        p.w0 = w0; p.h = step_h; p.bdiffw0 = bdiffw0; p.dt = dt;
+        p.max_err = max_pct_err; p.min_err = min_pct_err; p.sel = sel;
+        int rc = fill_desc(h, p, vc, &descs[b], nullptr);
+        if (rc) return rc;
+    }
+    int M = choose_M(n_points, 0);
+    int C = n_points / M;
+    if (n_pulses * C > 148)
+        return fail(h, OPTIFAX_ERR_UNSUPPORTED, "shared-schedule batch larger than one wave of SMs");
+    return launch_group(h, descs, M, C, method, vc, n_pulses > 1, st);
+}
+
+}  // extern "C"

@@ -1,0 +1,515 @@
+// ofx_pass.cuh -- the persistent crystal-pass kernel.
+//
+// One thread-block cluster of C CTAs propagates one pulse of N = C * M points
+// through the whole crystal in a single launch.  CTA rank c holds time points
+// [c M, (c+1) M) for the nonlinear sub-steps and, after the forward
+// transform, the spectral modes k = c + C k2 (k2 = 0..M-1).  Thread t owns
+// time points 16t .. 16t+15 of its CTA (held in registers across steps) and
+// spectral slots 16t .. 16t+15 (mode k2 = bitrev(slot)).
+//
+// Per step attempt (reference: OPO_CUDA_BATCH_XTAL.cu:432-506, Heun;
+// ode23/OPO_CUDA_ODE23.cu:446-538, RK23):
+//   RK stages: NL drive (A^2 e^{i phi} + 2|A|^2 e^{-i phi}, phi = w0 t - bdiffw0 z),
+//   shock-term central difference, stage combine -- all in registers, with
+//   the +-1 neighbours exchanged through shared memory (and distributed
+//   shared memory across the cluster).  Error classification (max-norm,
+//   percent) is an OR-reduction over the pulse (or over the batch when the
+//   reference's shared schedule is requested).  Accepted steps run the
+//   absorber, the forward FFT, the dispersion multiply, the inverse FFT and
+//   the 1/N scale without leaving the SM (cluster exchange for C > 1).
+//
+// Precision: FP32 field and FFT; phases exact in 64-bit fixed point (time
+// carrier w0 t, z carrier bdiffw0 z, accumulated dispersion beta z), applied
+// through FP32 sincospif; the dispersion factor of each step is
+// conj(g(z_old)) g(z_new) with g(z) = exp(-i beta z) so that rounding of the
+// unit factors telescopes instead of accumulating; the inverse FFT applies the
+// exact reciprocal of each forward twiddle.
+#pragma once
+#include <cooperative_groups.h>
+#include "ofx_fft.cuh"
+#include "../../include/optifax.h"
+
+namespace cg = cooperative_groups;
+
+namespace ofx {
+
+enum { TIME_SHIFTED = 0, TIME_UNSHIFTED = 1 };
+enum { ABC_SOFT = 0, ABC_NONE = 1, ABC_HARD = 2 };
+
+struct PulseDev {
+    const float2* E_in;
+    float2* A_out;
+    const float* alpha;
+    const float* beta;
+    const float* G;
+    float2* Ap;
+    float* stepmods;
+    int* trace;
+    const int* forced;
+    optifax_pulse_stats* stats;
+    double bdiffw0, dt;
+    uint64_t tau_theta;      // w0 dt in turns (fixed point)
+    uint64_t tau_z4;         // bdiffw0 h / 4 in turns (fixed point), per quarter step
+    float w0, h, max_err, min_err, sel, c_shock;
+    int N, S, nchunks, stepmods_limit, trace_cap, n_forced;
+};
+
+struct KernelCfg {
+    int time_mode;
+    int abc_mode;
+    int guard;           // XTAL/BATCH_OP: ceil chunk count and k < Nsteps loop guard
+    int shared_sched;    // 1: OR the error flags over every pulse of the launch (grid barrier)
+    int max_attempts_mul;
+    int* grid_flags;     // 3 ints (shared schedule only)
+};
+
+// ---------------------------------------------------------------------------
+// pointwise physics
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 nl_eval(float2 a, float2 cph, float2 z) {
+    float2 e = cmul(cph, z);
+    float ax2 = a.x * a.x, ay2 = a.y * a.y;
+    float2 a2 = make_float2(ax2 - ay2, 2.f * a.x * a.y);
+    float m2 = 2.f * (ax2 + ay2);
+    return make_float2(fmaf(a2.x, e.x, fmaf(-a2.y, e.y, m2 * e.x)),
+                       fmaf(a2.x, e.y, fmaf(a2.y, e.x, -m2 * e.y)));
+}
+
+// K = -i hG (NL - i cs (NL[+1] - NL[-1]))
+__device__ __forceinline__ float2 k_eval(float2 nlm, float2 nl0, float2 nlp, float hg, float cs) {
+    float2 d = csub(nlp, nlm);
+    float inx = fmaf(cs, d.y, nl0.x);
+    float iny = fmaf(-cs, d.x, nl0.y);
+    return make_float2(hg * iny, -hg * inx);
+}
+
+__device__ __forceinline__ int time_index(int i, int n, int mode) {
+    if (mode == TIME_SHIFTED) return (i > n / 2) ? i - n / 2 : i + n / 2;
+    return i;
+}
+
+__device__ __forceinline__ float abc_factor(int i, int n, int mode) {
+    if (mode == ABC_NONE) return 1.f;
+    int gi1 = 6 * (n / 16), gi2 = 10 * (n / 16);
+    if (!(i > gi1 && i < gi2)) return 1.f;
+    if (mode == ABC_HARD) return 0.f;
+    float pos = (48.f * fabsf((float)i - 0.5f * (float)n)) / (float)n;
+    float g = coshf(pos);
+    return 1.f - 1.f / (g * g);
+}
+
+__device__ __forceinline__ float2 zphase(uint64_t tau_z4, float pos) {
+    uint64_t p4 = (uint64_t)(4.0f * pos);
+    return turn_to_unit((uint64_t)0 - tau_z4 * p4);
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory layout
+// ---------------------------------------------------------------------------
+template <int M, int METHOD>
+struct Smem {
+    static constexpr int T = M / 16;
+    static constexpr int PADM = M + M / 16;
+    static constexpr int NBUF = (METHOD == OPTIFAX_RK23) ? 3 : 2;   // E, X (+K1 for RK23)
+    static constexpr size_t off_buf = 0;
+    static constexpr size_t off_tau = off_buf + sizeof(float2) * PADM * NBUF;
+    static constexpr size_t off_l2a = off_tau + sizeof(uint64_t) * M;
+    static constexpr size_t off_gq = off_l2a + sizeof(float) * M;
+    static constexpr size_t off_edge = off_gq + sizeof(float2) * M;
+    static constexpr size_t off_red = off_edge + sizeof(float2) * 4 * T;
+    static constexpr size_t bytes = off_red + 256;
+};
+
+// ---------------------------------------------------------------------------
+// cluster helpers
+// ---------------------------------------------------------------------------
+template <int C>
+__device__ __forceinline__ void csync() {
+    if constexpr (C > 1) cg::this_cluster().sync();
+    else __syncthreads();
+}
+
+template <int C, typename Tp>
+__device__ __forceinline__ Tp* remote(Tp* p, int rank) {
+    if constexpr (C > 1) return cg::this_cluster().map_shared_rank(p, rank);
+    else return p;
+}
+
+// Publish this thread's first/last stencil values and fetch the neighbours'.
+template <int M, int C>
+__device__ __forceinline__ void exchange_edges(float2* edge, int& par, int t, int c, float2 first,
+                                               float2 last, float2& left, float2& right) {
+    constexpr int T = M / 16;
+    float2* e = edge + par * 2 * T;
+    e[2 * t] = first;
+    e[2 * t + 1] = last;
+    csync<C>();
+    if (t > 0) left = e[2 * t - 1];
+    else left = remote<C>(e, (c + C - 1) % C)[2 * T - 1];
+    if (t < T - 1) right = e[2 * t + 2];
+    else right = remote<C>(e, (c + 1) % C)[0];
+    par ^= 1;
+}
+
+// N-point twiddle W_N^e for e in [0, N) from a half table
+__device__ __forceinline__ float2 twn_fwd(float2 v, const Twiddle* __restrict__ tw, int e, int half) {
+    if (e >= half) { float2 r = tw_fwd(v, tw[e - half]); return make_float2(-r.x, -r.y); }
+    return tw_fwd(v, tw[e]);
+}
+__device__ __forceinline__ float2 twn_inv(float2 v, const Twiddle* __restrict__ tw, int e, int half) {
+    if (e >= half) { float2 r = tw_inv(v, tw[e - half]); return make_float2(-r.x, -r.y); }
+    return tw_inv(v, tw[e]);
+}
+
+// Four-step split of the N = C M transform: forward step 1 (C-point DFTs
+// over CTAs, twiddle W_N^{n2 k1}) from every CTA's E buffer into the X
+// buffers; each CTA handles the n2 slice [c M/C, (c+1) M/C).
+template <int M, int C>
+__device__ __forceinline__ void exchange_forward(const float2* bufE, float2* bufX,
+                                                 const Twiddle* __restrict__ twN, int t, int c) {
+    if constexpr (C > 1) {
+        constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            int n2 = c * (M / C) + t + T * u;
+            float2 v[C];
+#pragma unroll
+            for (int n1 = 0; n1 < C; ++n1) v[n1] = remote<C>(bufE, n1)[phys(n2)];
+            dif_stages<N, C, C>(v, 0, twN);
+#pragma unroll
+            for (int r = 0; r < C; ++r) {
+                int k1 = bitrev(r, LOGC);
+                remote<C>(bufX, k1)[phys(n2)] = twn_fwd(v[r], twN, n2 * k1, N / 2);
+            }
+        }
+    }
+}
+
+// Inverse of exchange_forward: from every CTA's X buffer (local inverse
+// transforms, natural n2 order) back to the E buffers, scaled by 1/N.
+template <int M, int C>
+__device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* bufE,
+                                                 const Twiddle* __restrict__ twN, int t, int c, float invN) {
+    if constexpr (C > 1) {
+        constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            int n2 = c * (M / C) + t + T * u;
+            float2 v[C];
+#pragma unroll
+            for (int r = 0; r < C; ++r) {
+                int k1 = bitrev(r, LOGC);
+                v[r] = twn_inv(remote<C>(bufX, k1)[phys(n2)], twN, n2 * k1, N / 2);
+            }
+            dit_stages<N, C, C>(v, 0, twN);
+#pragma unroll
+            for (int n1 = 0; n1 < C; ++n1) remote<C>(bufE, n1)[phys(n2)] = cscale(v[n1], invN);
+        }
+    }
+}
+
+// OR of per-thread flag bits over the CTA, the cluster and (shared schedule)
+// the grid.  red[0..2] CTA slots (triple buffered by attempt), red[4..4+2*16)
+// cluster slots (double buffered).
+template <int M, int C>
+__device__ __forceinline__ int reduce_flags(int bits, int* red, int attempt, int t, int c,
+                                            const KernelCfg& cfg) {
+    int w = __reduce_or_sync(0xffffffffu, bits);
+    int slot = attempt % 3;
+    if ((t & 31) == 0 && w) atomicOr(&red[slot], w);
+    __syncthreads();
+    int f = red[slot];
+    if constexpr (C > 1) {
+        int* cl = red + 4 + (attempt & 1) * 16;
+        if (t == 0) {
+#pragma unroll 1
+            for (int r = 0; r < C; ++r) remote<C>(cl, r)[c] = f;
+        }
+        cg::this_cluster().sync();
+        f = 0;
+#pragma unroll 1
+        for (int r = 0; r < C; ++r) f |= cl[r];
+    }
+    if (cfg.shared_sched) {
+        int gslot = attempt % 3;
+        if (t == 0 && c == 0 && f) atomicOr(&cfg.grid_flags[gslot], f);
+        cg::this_grid().sync();
+        f = *((volatile int*)&cfg.grid_flags[gslot]);
+        if (blockIdx.x == 0 && t == 0) cfg.grid_flags[(attempt + 2) % 3] = 0;
+    }
+    if (t == 0) red[(attempt + 2) % 3] = 0;
+    return f;
+}
+
+// ---------------------------------------------------------------------------
+// the kernel
+// ---------------------------------------------------------------------------
+template <int M, int C, int METHOD>
+__global__ void __launch_bounds__(M / 16, 1)
+pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM,
+            const Twiddle* __restrict__ twN, KernelCfg cfg) {
+    constexpr int T = M / 16;
+    constexpr int N = M * C;
+    constexpr int LOG2M = FftShape<M>::LOG2M;
+    using SM = Smem<M, METHOD>;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* bufE = reinterpret_cast<float2*>(smem + SM::off_buf);
+    float2* bufX = bufE + SM::PADM;
+    float2* bufK = bufX + SM::PADM;   // RK23 only: FSAL K1 (own points)
+    uint64_t* tau_s = reinterpret_cast<uint64_t*>(smem + SM::off_tau);
+    float* l2a_s = reinterpret_cast<float*>(smem + SM::off_l2a);
+    float2* gq_s = reinterpret_cast<float2*>(smem + SM::off_gq);
+    float2* edge = reinterpret_cast<float2*>(smem + SM::off_edge);
+    int* red = reinterpret_cast<int*>(smem + SM::off_red);
+
+    const int t = threadIdx.x;
+    const int c = (C > 1) ? (int)cg::this_cluster().block_rank() : 0;
+    const int p = blockIdx.x / C;
+    const PulseDev& P = pulses[p];
+
+    // ---- prologue -------------------------------------------------------
+    if (t < 64) red[t] = 0;
+    float2 cph[16], a[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        int i = c * M + 16 * t + j;
+        uint64_t jt = (uint64_t)time_index(i, N, cfg.time_mode);
+        cph[j] = turn_to_unit(P.tau_theta * jt);
+        a[j] = P.E_in[i];
+    }
+#pragma unroll 1
+    for (int j = 0; j < 16; ++j) {
+        int slot = 16 * t + j;
+        int k = c + C * bitrev(slot, LOG2M);
+        double b = (double)P.beta[k];
+        double r = b - 6.283185307179586 * rint(b * 0.15915494309189535);
+        double x = r * 2.9357677120600766e18;          // 2^64 / (2 pi)
+        if (x >= 9.2233720368547758e18) x -= 1.8446744073709552e19;
+        if (x < -9.2233720368547758e18) x += 1.8446744073709552e19;
+        tau_s[j * T + t] = (uint64_t)(long long)llrint(x);
+        l2a_s[j * T + t] = log2f(P.alpha[k]);
+        gq_s[j * T + t] = make_float2(1.f, 0.f);
+    }
+    if constexpr (C > 1) cg::this_cluster().sync(); else __syncthreads();
+
+    const float* G = P.G;
+    const float h = P.h, sel = P.sel, cs = P.c_shock, Sf = (float)P.S;
+    const float maxE = P.max_err, minE = P.min_err;
+    const float invN = 1.0f / (float)N;
+    const int guard = cfg.guard;
+    const long long max_attempts = (long long)cfg.max_attempts_mul * (long long)(P.S + 16) + 64;
+
+    float k = 0.f, stepprev = 4.f, stepmod = 4.f;
+    unsigned q = 0;                          // accumulated dispersion position (sum of stepmod)
+    int attempt = 0, n_acc = 0, n_rej = 0, status = 0, par = 0;
+    const bool rec = (c == 0 && t == 0);
+
+    // RK23 carries K1 (first stage, FSAL) between attempts in registers
+    float2 k1r[16];
+    if constexpr (METHOD == OPTIFAX_RK23) {
+        // initial K1 at k = 0 with stepmod = 4 (OPO_CUDA_ODE23.cu:432-438)
+        float hg = (stepmod * h) * G[0];
+        float2 z = zphase(P.tau_z4, 0.f);
+        float2 nl[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
+        float2 L, R;
+        exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            k1r[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+    }
+
+    const int nchunks = P.nchunks;
+    for (int chunk = 0; chunk < nchunks; ++chunk) {
+        stepmod = stepprev;
+        const float cend = (float)(chunk + 1) * sel;
+        while (k < cend && (!guard || k < Sf)) {
+            if (attempt >= max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; goto done; }
+            const int kidx = (int)k;
+            const float hmod = stepmod * h;
+            const float hg = hmod * G[kidx];
+            int bits = 0;
+            if constexpr (METHOD == OPTIFAX_HEUN) {
+                // ---- stage 1: K1 = f(A0) at z = k ----
+                float2 nl[16], k1[16], L, R;
+                float2 z = zphase(P.tau_z4, k);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
+                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    k1[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                // ---- stage 2: K2 = f(A0 + K1) at z = k + stepmod ----
+                z = zphase(P.tau_z4, k + stepmod);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], k1[j]), cph[j], z);
+                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float2 k2 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                    float2 e = cadd(a[j], cadd(cscale(k2, 0.5f), cscale(k1[j], 0.5f)));
+                    float2 d = cscale(csub(k2, k1[j]), 0.5f);          // = E - A1
+                    float ae = cabsf2(e);
+                    if (ae > 0.f) {
+                        float pct = 100.f * (cabsf2(d) / (ae + 1.f));
+                        if (pct >= maxE) bits |= 1;
+                        else if (pct >= minE) bits |= 2;
+                    }
+                    if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
+                    int i = c * M + 16 * t + j;
+                    bufE[phys(16 * t + j)] = cscale(e, abc_factor(i, N, cfg.abc_mode));
+                }
+            } else {
+                // ---- RK23: stage 2 (K2 at k + s/2), stage 3 (K3 at k + 3s/4), stage 4 (K4 at k + s)
+                float2 nl[16], k2[16], pp[16], L, R;
+                float2 z = zphase(P.tau_z4, k + 0.5f * stepmod);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], cscale(k1r[j], 0.5f)), cph[j], z);
+                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    k2[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                z = zphase(P.tau_z4, k + 0.75f * stepmod);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], cscale(k2[j], 0.75f)), cph[j], z);
+                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+                float2 ev[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float2 k3 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                    float2 e = cadd(a[j], cadd(cscale(k3, 4.f / 9.f), cscale(k2[j], 1.f / 3.f)));
+                    ev[j] = cadd(e, cscale(k1r[j], 2.f / 9.f));
+                    // E - A1 without K4: (4/9-1/3) K3 + (1/3-1/4) K2 + (2/9-7/24) K1
+                    pp[j] = cadd(cadd(cscale(k3, 1.f / 9.f), cscale(k2[j], 1.f / 12.f)),
+                                 cscale(k1r[j], -5.f / 72.f));
+                }
+                z = zphase(P.tau_z4, k + stepmod);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(ev[j], cph[j], z);
+                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float2 k4 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                    float2 d = csub(pp[j], cscale(k4, 1.f / 8.f));  // = E - A1
+                    float ae = cabsf2(ev[j]);
+                    if (ae > 0.f) {
+                        float pct = 200.f * (cabsf2(d) / (ae + 1.f));
+                        if (pct >= maxE) bits |= 1;
+                        else if (pct >= minE) bits |= 2;
+                    }
+                    if (!(isfinite(ev[j].x) && isfinite(ev[j].y))) bits |= 4;
+                    int i = c * M + 16 * t + j;
+                    bufE[phys(16 * t + j)] = cscale(ev[j], abc_factor(i, N, cfg.abc_mode));
+                    bufK[phys(16 * t + j)] = k4;   // FSAL candidate (own points)
+                }
+            }
+
+            int fl = reduce_flags<M, C>(bits, red, attempt, t, c, cfg);
+            if (P.forced && attempt < P.n_forced) fl = (P.forced[attempt] & 3) | (fl & 4);
+            if (fl & 4) status |= OPTIFAX_PULSE_NAN;
+
+            if ((fl & 1) && stepmod > 1.f && (k - stepmod) > 0.f) {
+                // ---- reject: A0 unchanged; k moves back by one in net (the loop adds the new stepmod)
+                if (rec && P.trace && attempt < P.trace_cap) {
+                    P.trace[3 * attempt] = kidx; P.trace[3 * attempt + 1] = (int)stepmod;
+                    P.trace[3 * attempt + 2] = fl & 7;
+                }
+                ++n_rej;
+                k = k - stepmod;
+                stepmod = stepmod - 1.f;
+                stepprev = stepmod;
+                if constexpr (METHOD == OPTIFAX_RK23) {
+                    // K1 recomputed at z = k + stepmod with G[k] (OPO_CUDA_ODE23.cu:484-487)
+                    float hg1 = (stepmod * h) * G[(int)k];
+                    float2 z = zphase(P.tau_z4, k + stepmod);
+                    float2 nl[16], L, R;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
+                    exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        k1r[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg1, cs);
+                }
+            } else {
+                // ---- accept ----
+                if (rec && P.trace && attempt < P.trace_cap) {
+                    P.trace[3 * attempt] = kidx; P.trace[3 * attempt + 1] = (int)stepmod;
+                    P.trace[3 * attempt + 2] = (fl & 7) | 8;
+                }
+                ++n_acc;
+                const int s_used = (int)stepmod;
+                if (rec && P.stepmods && kidx < P.stepmods_limit && kidx < P.S) P.stepmods[kidx] = (float)s_used;
+                // step control (OPO_CUDA_BATCH_XTAL.cu:487-506; ODE23 :519-538 doubles)
+                if (k + stepmod >= cend && k < cend - 1.f) {
+                    float stepend = (cend - k) - 1.f;
+                    stepprev = stepmod;
+                    stepmod = stepend;
+                } else {
+                    if constexpr (METHOD == OPTIFAX_HEUN) {
+                        if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.f) < cend - 1.f) stepmod = stepmod + 1.f;
+                    } else {
+                        if (!(fl & 2) && !(fl & 1) && (k + stepmod + stepmod) < cend - 1.f) stepmod = stepmod * 2.f;
+                    }
+                    stepprev = stepmod;
+                }
+                const float knext = k + stepmod;
+                const bool last_in_chunk = !(knext < cend && (!guard || knext < Sf));
+                const unsigned qn = q + (unsigned)s_used;
+
+                // ---- linear sub-step: FFT, dispersion, inverse FFT ----
+                float2* fbuf = (C > 1) ? bufX : bufE;
+                if constexpr (C > 1) {
+                    exchange_forward<M, C>(bufE, bufX, twN, t, c);
+                    cg::this_cluster().sync();
+                } else {
+                    __syncthreads();
+                }
+                float2 v[16];
+                fft_forward_to_regs<M>(fbuf, twM, t, v);
+                float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    uint64_t ph = tau_s[j * T + t] * (uint64_t)qn;
+                    float2 gn = turn_to_unit((uint64_t)0 - ph);
+                    float2 go = gq_s[j * T + t];
+                    float amp = exp2f((float)s_used * l2a_s[j * T + t]);
+                    float2 f = cmulc(gn, go);
+                    v[j] = cscale(cmul(v[j], f), amp);
+                    gq_s[j * T + t] = gn;
+                    if (apc) apc[c + C * bitrev(16 * t + j, LOG2M)] = v[j];
+                }
+                fft_inverse_from_regs<M>(fbuf, twM, t, v);
+                if constexpr (C > 1) {
+                    cg::this_cluster().sync();
+                    exchange_inverse<M, C>(bufX, bufE, twN, t, c, invN);
+                    cg::this_cluster().sync();
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) a[j] = bufE[phys(16 * t + j)];
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) a[j] = cscale(bufE[phys(16 * t + j)], invN);
+                }
+                if constexpr (METHOD == OPTIFAX_RK23) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) k1r[j] = bufK[phys(16 * t + j)];
+                }
+                q = qn;
+            }
+            ++attempt;
+            k = k + stepmod;
+        }
+    }
+done:
+#pragma unroll
+    for (int j = 0; j < 16; ++j) P.A_out[c * M + 16 * t + j] = a[j];
+    if (rec && P.stats) {
+        optifax_pulse_stats st;
+        st.attempts = attempt; st.accepted = n_acc; st.rejected = n_rej; st.status = status;
+        st.z_steps = (long long)q; st.k_final = k; st.stepmod_final = stepmod; st.n_chunks = nchunks;
+        st.reserved[0] = st.reserved[1] = st.reserved[2] = 0;
+        *P.stats = st;
+    }
+}
+
+}  // namespace ofx

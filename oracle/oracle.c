@@ -1,0 +1,579 @@
+/*
+ * oracle.c -- FP64 CPU restatement of OptiFax's chi(2) crystal-pass solver.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU propagator
+ * in optifax_gb300/csrc/.  Only tests/, __graft_entry__.smoke() and bench.py
+ * (its cpu_baseline leg and its --impl reference arm) may load it.  The
+ * product path never calls it.
+ *
+ * Parity status: UNPINNED.  The reference ships no golden vectors, fixtures or
+ * tests for this path, and its own implementations (MATLAB NEE_CPU.m and the
+ * MATLAB MEX wrapper around OPO_CUDA_*.cu) cannot run in this environment.
+ * The restatement is instead checked by known-answer tests (pure dispersion,
+ * undepleted-pump sinc^2 gain, Manley-Rowe/energy conservation, convergence
+ * order) in tests/test_oracle.py.
+ *
+ * Three schedules are restated, each in double precision, with every input
+ * value taken exactly as the reference receives it (w0, h, G, beta, alpha are
+ * FP32 values in the reference; they arrive here already rounded):
+ *
+ *   OFX_ORACLE_HEUN_MEX  toolbox/lib/MEXlib/src/OPO_CUDA_BATCH_XTAL.cu:373-525
+ *                        (host driver), kernels :142-305.  Variants:
+ *                        OPO_CUDA_BATCH_OP.cu (shared poling G[k], :221),
+ *                        OPO_CUDA_NO_BC.cu (unshifted time :172, no absorber
+ *                        :399-402, truncated chunk count, no k<Nsteps guard),
+ *                        OPO_CUDA_HARD_BC.cu (hard absorber :118-129).
+ *   OFX_ORACLE_RK23_MEX  toolbox/lib/MEXlib/src/ode23/OPO_CUDA_ODE23.cu:375-557
+ *                        (Bogacki-Shampine 3(2) with FSAL taken before the
+ *                        dispersion sub-step, step doubling).
+ *   OFX_ORACLE_HEUN_NEE  toolbox/lib/internal/main/NEE_CPU.m:1-122 (the
+ *                        MATLAB CPU solver, plotting removed).
+ *
+ * The FFT is a plain radix-2 FP64 transform of our own (FFTW, which MATLAB
+ * uses, and cuFFT, which the MEX uses, are closed binaries and neither is
+ * available here); any transform exact to FP64 rounding is equivalent.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdint.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "oracle.h"
+
+typedef struct { double re, im; } cplx;
+
+static inline cplx cmk(double r, double i) { cplx z = {r, i}; return z; }
+static inline cplx cadd(cplx a, cplx b) { return cmk(a.re + b.re, a.im + b.im); }
+static inline cplx csub(cplx a, cplx b) { return cmk(a.re - b.re, a.im - b.im); }
+static inline cplx cmul(cplx a, cplx b) {
+    return cmk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+static inline cplx cscale(cplx a, double s) { return cmk(a.re * s, a.im * s); }
+static inline cplx cconj(cplx a) { return cmk(a.re, -a.im); }
+static inline double cabs2(cplx a) { return hypot(a.re, a.im); }
+static inline cplx cexpi(double phi) { return cmk(cos(phi), sin(phi)); }
+
+/* ------------------------------------------------------------------------ */
+/* FFT: iterative radix-2, in place, unnormalised, sign -1 forward.          */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int n, log2n;
+    cplx* tw;       /* exp(-2 pi i e / n), e in [0, n/2) */
+    int* rev;       /* bit reversal permutation */
+} fft_plan;
+
+static int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
+
+static int fft_plan_init(fft_plan* p, int n) {
+    p->n = n; p->log2n = ilog2(n);
+    if ((1 << p->log2n) != n) return -1;
+    p->tw = (cplx*)malloc(sizeof(cplx) * (size_t)(n / 2 + 1));
+    p->rev = (int*)malloc(sizeof(int) * (size_t)n);
+    if (!p->tw || !p->rev) return -2;
+    for (int e = 0; e < n / 2; ++e) {
+        /* angle in turns computed exactly, then to radians */
+        double a = -2.0 * M_PI * (double)e / (double)n;
+        p->tw[e] = cmk(cos(a), sin(a));
+    }
+    for (int i = 0; i < n; ++i) {
+        int r = 0;
+        for (int b = 0; b < p->log2n; ++b) if (i & (1 << b)) r |= 1 << (p->log2n - 1 - b);
+        p->rev[i] = r;
+    }
+    return 0;
+}
+
+static void fft_plan_free(fft_plan* p) { free(p->tw); free(p->rev); }
+
+static void fft_exec(const fft_plan* p, cplx* x, int inverse) {
+    const int n = p->n;
+    for (int i = 0; i < n; ++i) {
+        int r = p->rev[i];
+        if (r > i) { cplx t = x[i]; x[i] = x[r]; x[r] = t; }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        int half = len >> 1, step = n / len;
+        for (int b = 0; b < n; b += len) {
+            for (int j = 0; j < half; ++j) {
+                cplx w = p->tw[j * step];
+                if (inverse) w = cconj(w);
+                cplx u = x[b + j], v = cmul(x[b + j + half], w);
+                x[b + j] = cadd(u, v);
+                x[b + j + half] = csub(u, v);
+            }
+        }
+    }
+}
+
+int ofx_oracle_fft(const double* in, double* out, int n, int inverse) {
+    fft_plan p;
+    if (fft_plan_init(&p, n)) { fft_plan_free(&p); return OFX_ORACLE_EINVAL; }
+    memcpy(out, in, sizeof(double) * 2 * (size_t)n);
+    fft_exec(&p, (cplx*)out, inverse);
+    fft_plan_free(&p);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Physics pieces shared by the schedules                                    */
+/* ------------------------------------------------------------------------ */
+
+/* Sample time used by the nonlinear drive for array index i.
+ *   shifted:   OPO_CUDA_BATCH_XTAL.cu:173-180  t = (i +- N/2) dt
+ *   unshifted: OPO_CUDA_NO_BC.cu:172, OPO_CUDA_ODE23.cu:176  t = i dt
+ *   nee:       NEE_CPU.m:12,53  t = fftshift((-N/2:N/2-1) dt)            */
+static double sample_time(int mode, int i, int n, double dt) {
+    if (mode == OFX_TIME_SHIFTED) {
+        if (i > n / 2) return dt * (double)(i - n / 2);
+        return dt * (double)(i + n / 2);
+    } else if (mode == OFX_TIME_UNSHIFTED) {
+        return dt * (double)i;
+    } else {
+        return (i < n / 2) ? dt * (double)i : dt * (double)(i - n);
+    }
+}
+
+/* NL = A^2 e^{i phi} + 2 |A|^2 e^{-i phi},  phi = w0 t_i - bdwz
+ * (OPO_CUDA_BATCH_XTAL.cu:182-187; NEE_CPU.m:98-101). */
+static void nl_eval(const cplx* A, cplx* NL, int n, const double* tw0, double bdwz) {
+    for (int i = 0; i < n; ++i) {
+        cplx e = cexpi(tw0[i] - bdwz);
+        cplx a = A[i];
+        double m = cabs2(a);
+        cplx a2 = cmul(a, a);
+        NL[i] = cadd(cmul(a2, e), cscale(cconj(e), 2.0 * m * m));
+    }
+}
+
+/* K = -i h G (NL - i/(2 dt w0) (NL[i+1] - NL[i-1])), periodic neighbours
+ * (OPO_CUDA_BATCH_XTAL.cu:221-249; NEE_CPU.m:103-105). */
+static void k_eval(const cplx* NL, cplx* K, int n, double hmod, double g, double c_shock) {
+    for (int i = 0; i < n; ++i) {
+        int ip = (i + 1 == n) ? 0 : i + 1;
+        int im = (i == 0) ? n - 1 : i - 1;
+        cplx d = csub(NL[ip], NL[im]);
+        /* i * c_shock * d */
+        cplx id = cmk(-c_shock * d.im, c_shock * d.re);
+        cplx in = csub(NL[i], id);
+        /* -i * hG * in */
+        double hg = hmod * g;
+        K[i] = cmk(hg * in.im, -hg * in.re);
+    }
+}
+
+/* Absorbing boundary factor for array index i (OPO_CUDA_BATCH_XTAL.cu:105-137,
+ * window gi1 = 6(N/16), gi2 = 10(N/16) at :412-413; HARD_BC: factor 0 with
+ * a=2; NO_BC: gi1 = gi2 = 0, i.e. no points). */
+static double abc_factor_mex(int mode, int i, int n) {
+    if (mode == OFX_ABC_NONE) return 1.0;
+    int gi1 = 6 * (n / 16), gi2 = 10 * (n / 16);
+    if (!(i > gi1 && i < gi2)) return 1.0;
+    if (mode == OFX_ABC_HARD) return 0.0;
+    double pos = (24.0 * 2.0 / (double)n) * fabs((double)i - (double)n / 2.0);
+    double g = cosh(pos);
+    return 1.0 - 1.0 / (g * g);
+}
+
+/* NEE_CPU.m:114-121: t_idx = range(t) - |2t| < b range(t), factor
+ * 1 - sech(a (1 - |2t|/range(t)))^2, a = 24, b = 0.25, t = fftshift(t). */
+static double abc_factor_nee(int i, int n, double dt) {
+    double t = sample_time(OFX_TIME_NEE, i, n, dt);
+    double range = (double)(n - 1) * dt;
+    double a2t = fabs(2.0 * t);
+    if (!(range - a2t < 0.25 * range)) return 1.0;
+    double s = 1.0 / cosh(24.0 * (1.0 - a2t / range));
+    return 1.0 - s * s;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Schedules                                                                 */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    const ofx_oracle_params* p;
+    int b0, nb;                 /* pulses in this schedule */
+    const cplx* E_in;
+    const double* alpha;
+    const double* G;
+    const double* beta;
+    cplx* A_out;
+    cplx* Ap; long long ap_len;
+    double* stepmods;
+    int* trace; int trace_cap; int* n_attempts;
+    const int* forced; int n_forced;
+    ofx_oracle_stats* stats;
+} sched_ctx;
+
+typedef struct {
+    int n;
+    fft_plan plan;
+    cplx *A0, *A1, *E, *NL, *K1, *K2, *K3, *K4;
+    double* tw0;
+} work;
+
+static int work_init(work* w, int n, int nb, int time_mode, double w0, double dt) {
+    memset(w, 0, sizeof(*w));
+    w->n = n;
+    if (fft_plan_init(&w->plan, n)) return -1;
+    size_t sz = sizeof(cplx) * (size_t)n * (size_t)nb;
+    w->A0 = (cplx*)malloc(sz); w->A1 = (cplx*)malloc(sz); w->E = (cplx*)malloc(sz);
+    w->NL = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+    w->K1 = (cplx*)malloc(sz); w->K2 = (cplx*)malloc(sz);
+    w->K3 = (cplx*)malloc(sz); w->K4 = (cplx*)malloc(sz);
+    w->tw0 = (double*)malloc(sizeof(double) * (size_t)n);
+    if (!w->A0 || !w->A1 || !w->E || !w->NL || !w->K1 || !w->K2 || !w->K3 || !w->K4 || !w->tw0)
+        return -2;
+    for (int i = 0; i < n; ++i) w->tw0[i] = w0 * sample_time(time_mode, i, n, dt);
+    return 0;
+}
+
+static void work_free(work* w) {
+    fft_plan_free(&w->plan);
+    free(w->A0); free(w->A1); free(w->E); free(w->NL);
+    free(w->K1); free(w->K2); free(w->K3); free(w->K4); free(w->tw0);
+}
+
+static double g_at(const sched_ctx* c, int k, int b) {
+    const ofx_oracle_params* p = c->p;
+    if (k < 0) k = 0;
+    if (k >= p->S) k = p->S - 1;
+    return p->g_per_pulse ? c->G[(size_t)k + (size_t)(c->b0 + b) * (size_t)p->S] : c->G[k];
+}
+
+/* one NL+K stage for every pulse of the schedule: K = f(X) */
+static void stage(const sched_ctx* c, work* w, const cplx* X, cplx* K, double pos,
+                  double hmod, int kidx) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N;
+    double bdwz = p->bdiffw0 * pos * p->h;
+    double c_shock = 1.0 / (2.0 * p->dt * p->w0);
+    for (int b = 0; b < c->nb; ++b) {
+        nl_eval(X + (size_t)b * n, w->NL, n, w->tw0, bdwz);
+        k_eval(w->NL, K + (size_t)b * n, n, hmod, g_at(c, kidx, b), c_shock);
+    }
+}
+
+/* error classification over all pulses of the schedule:
+ * OPO_CUDA_BATCH_XTAL.cu:325-349 (pct = 100 |E-A1|/(|E|+1), >= maxErr sets
+ * flag0, else >= minErr sets flag1, points with |E| == 0 skipped);
+ * ODE23 uses 4*100*0.5*|E-A1| (OPO_CUDA_ODE23.cu:332-335). */
+static int classify(const sched_ctx* c, const cplx* E, const cplx* A1, double scale,
+                    double* pct_max_out) {
+    const ofx_oracle_params* p = c->p;
+    int flags = 0; double pm = 0.0;
+    size_t tot = (size_t)p->N * (size_t)c->nb;
+    for (size_t i = 0; i < tot; ++i) {
+        double ae = cabs2(E[i]);
+        if (ae > 0) {
+            double pct = scale * cabs2(csub(E[i], A1[i])) / (ae + 1.0);
+            if (pct > pm) pm = pct;
+            if (pct >= p->maxErr) flags |= 1;
+            else if (pct >= p->minErr) flags |= 2;
+        }
+        if (isnan(E[i].re) || isnan(E[i].im)) flags |= 4;
+    }
+    *pct_max_out = pm;
+    return flags;
+}
+
+static void record(sched_ctx* c, int attempt, int k, int s, int flags, int accepted) {
+    if (c->trace && attempt < c->trace_cap) {
+        c->trace[3 * attempt + 0] = k;
+        c->trace[3 * attempt + 1] = s;
+        c->trace[3 * attempt + 2] = (flags & 3) | (accepted ? 8 : 0) | (flags & 4);
+    }
+}
+
+/* accepted step's linear sub-step: absorber, FFT, dispersion x stepmod, snapshot,
+ * stepmods record, IFFT, 1/N  (OPO_CUDA_BATCH_XTAL.cu:469-485, :255-305). */
+static void dispersion_step(sched_ctx* c, work* w, cplx* E, cplx* A0, int s, int chunk,
+                            int nchunks, int k) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N;
+    double inv_n = 1.0 / (double)n;
+    for (int b = 0; b < c->nb; ++b) {
+        cplx* e = E + (size_t)b * n;
+        for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_mex(p->abc_mode, i, n));
+        fft_exec(&w->plan, e, 0);
+        for (int i = 0; i < n; ++i) {
+            cplx f = cscale(cexpi(-c->beta[i] * (double)s), pow(c->alpha[i], (double)s));
+            e[i] = cmul(e[i], f);
+        }
+        if (c->Ap) {
+            long long off = ((long long)(c->b0 + b) * nchunks + chunk) * (long long)n;
+            if (off >= 0 && off + n <= c->ap_len) memcpy(c->Ap + off, e, sizeof(cplx) * (size_t)n);
+            else c->stats->status |= OFX_ORACLE_STATUS_AP_RANGE;
+        }
+        fft_exec(&w->plan, e, 1);
+        cplx* a0 = A0 + (size_t)b * n;
+        for (int i = 0; i < n; ++i) a0[i] = cscale(e[i], inv_n);
+    }
+    if (c->stepmods && k < p->stepmods_limit && k < p->S && k >= 0) c->stepmods[k] = (double)s;
+}
+
+static int get_flags(sched_ctx* c, int attempt, int computed) {
+    if (c->forced && attempt < c->n_forced) return (c->forced[attempt] & 3) | (computed & 4);
+    return computed;
+}
+
+/* OPO_CUDA_BATCH_XTAL.cu:373-525 and its variants */
+static void run_heun_mex(sched_ctx* c, work* w) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N;
+    const double sel = p->sel;
+    double k = 0.0, stepprev = 4.0, stepmod = stepprev, stepend;
+    int nchunks = (int)((double)p->S / sel);
+    if (p->chunk_mode == OFX_CHUNKS_CEIL && (double)nchunks * sel < (double)p->S) nchunks += 1;
+    int attempt = 0;
+    double pm;
+    for (int chunk = 0; chunk < nchunks; ++chunk) {
+        stepmod = stepprev;
+        double cend = (double)(chunk + 1) * sel;
+        for (; k < cend && (p->chunk_mode != OFX_CHUNKS_CEIL || k < (double)p->S); k = k + stepmod) {
+            int kidx = (int)k;
+            double hmod = stepmod * p->h;
+            stage(c, w, w->A0, w->K1, k, hmod, kidx);
+            size_t tot = (size_t)n * c->nb;
+            for (size_t i = 0; i < tot; ++i)
+                w->A1[i] = cadd(w->A0[i], cadd(cscale(w->K1[i], 0.5), cscale(w->K1[i], 0.5)));
+            stage(c, w, w->A1, w->K2, k + stepmod, hmod, kidx);
+            for (size_t i = 0; i < tot; ++i)
+                w->E[i] = cadd(w->A0[i], cadd(cscale(w->K2[i], 0.5), cscale(w->K1[i], 0.5)));
+            int fl = classify(c, w->E, w->A1, 100.0, &pm);
+            fl = get_flags(c, attempt, fl);
+            if (fl & 4) c->stats->status |= OFX_ORACLE_STATUS_NAN;
+            c->stats->pct_max_last = pm;
+            if ((fl & 1) && stepmod > 1.0 && (k - stepmod) > 0.0) {
+                record(c, attempt, kidx, (int)stepmod, fl, 0);
+                c->stats->rejected++;
+                k = k - stepmod;
+                stepmod = stepmod - 1.0;
+                stepprev = stepmod;
+            } else {
+                record(c, attempt, kidx, (int)stepmod, fl, 1);
+                c->stats->accepted++;
+                c->stats->z_steps += (long long)stepmod;
+                dispersion_step(c, w, w->E, w->A0, (int)stepmod, chunk, nchunks, kidx);
+                if (k + stepmod >= cend && k < cend - 1.0) {
+                    stepend = (cend - k) - 1.0;
+                    stepprev = stepmod;
+                    stepmod = stepend;
+                } else {
+                    if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.0) < cend - 1.0)
+                        stepmod = stepmod + 1.0;
+                    stepprev = stepmod;
+                }
+            }
+            attempt++;
+        }
+    }
+    c->stats->attempts = attempt;
+    c->stats->k_final = k;
+    c->stats->stepmod_final = stepmod;
+    c->stats->nchunks = nchunks;
+    if (c->n_attempts) *c->n_attempts = attempt;
+}
+
+/* OPO_CUDA_ODE23.cu:375-557 */
+static void run_rk23_mex(sched_ctx* c, work* w) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N;
+    const double sel = p->sel;
+    const size_t tot = (size_t)n * c->nb;
+    double k = 0.0, stepprev = 4.0, stepmod = stepprev, stepend;
+    int nchunks = (int)((double)p->S / sel);
+    if (p->chunk_mode == OFX_CHUNKS_CEIL && (double)nchunks * sel < (double)p->S) nchunks += 1;
+    int attempt = 0;
+    double pm;
+    cplx *K1 = w->K1, *K4 = w->K4;
+    stepmod = stepprev;
+    /* initial K1 at k = 0 (:432-438) */
+    stage(c, w, w->A0, K1, k, stepmod * p->h, 0);
+    for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
+    for (int chunk = 0; chunk < nchunks; ++chunk) {
+        stepmod = stepprev;
+        double cend = (double)(chunk + 1) * sel;
+        for (; k < cend && (p->chunk_mode != OFX_CHUNKS_CEIL || k < (double)p->S); k = k + stepmod) {
+            int kidx = (int)k;
+            double hmod = stepmod * p->h;
+            stage(c, w, w->A1, w->K2, k + 0.5 * stepmod, hmod, kidx);
+            for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(w->K2[i], 0.75));
+            stage(c, w, w->A1, w->K3, k + 0.75 * stepmod, hmod, kidx);
+            for (size_t i = 0; i < tot; ++i) {
+                cplx e = cadd(w->A0[i], cadd(cscale(w->K3[i], 4.0 / 9.0), cscale(w->K2[i], 1.0 / 3.0)));
+                w->E[i] = cadd(e, cscale(K1[i], 2.0 / 9.0));
+            }
+            stage(c, w, w->E, K4, k + stepmod, hmod, kidx);
+            for (size_t i = 0; i < tot; ++i) {
+                cplx a = cadd(w->A0[i], cadd(cscale(K4[i], 1.0 / 8.0), cscale(w->K3[i], 1.0 / 3.0)));
+                a = cadd(a, cscale(w->K2[i], 1.0 / 4.0));
+                w->A1[i] = cadd(a, cscale(K1[i], 7.0 / 24.0));
+            }
+            int fl = classify(c, w->E, w->A1, 200.0, &pm);
+            fl = get_flags(c, attempt, fl);
+            if (fl & 4) c->stats->status |= OFX_ORACLE_STATUS_NAN;
+            c->stats->pct_max_last = pm;
+            if ((fl & 1) && stepmod > 1.0 && (k - stepmod) > 0.0) {
+                record(c, attempt, kidx, (int)stepmod, fl, 0);
+                c->stats->rejected++;
+                k = k - stepmod;
+                stepmod = stepmod - 1.0;
+                stepprev = stepmod;
+                /* K1 recomputed at the new start, G index k (:484-487) */
+                stage(c, w, w->A0, K1, k + stepmod, stepmod * p->h, (int)k);
+                for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
+            } else {
+                record(c, attempt, kidx, (int)stepmod, fl, 1);
+                c->stats->accepted++;
+                c->stats->z_steps += (long long)stepmod;
+                dispersion_step(c, w, w->E, w->A0, (int)stepmod, chunk, nchunks, kidx);
+                cplx* t = K1; K1 = K4; K4 = t;     /* FSAL swap (:512-514) */
+                for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
+                if (k + stepmod >= cend && k < cend - 1.0) {
+                    stepend = (cend - k) - 1.0;
+                    stepprev = stepmod;
+                    stepmod = stepend;
+                } else {
+                    if (!(fl & 2) && !(fl & 1) && (k + stepmod + stepmod) < cend - 1.0)
+                        stepmod = stepmod * 2.0;
+                    stepprev = stepmod;
+                }
+            }
+            attempt++;
+        }
+    }
+    c->stats->attempts = attempt;
+    c->stats->k_final = k;
+    c->stats->stepmod_final = stepmod;
+    c->stats->nchunks = nchunks;
+    if (c->n_attempts) *c->n_attempts = attempt;
+}
+
+/* NEE_CPU.m:1-122 (B = 1 per schedule; G33 indexed 1-based by k). */
+static void run_heun_nee(sched_ctx* c, work* w) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N;
+    const size_t tot = (size_t)n * c->nb;
+    double k = 1.0, stepmod = 4.0;
+    double nchunks_d = (double)p->S / p->sel;
+    int nchunks = (int)floor(nchunks_d);          /* for chunk = 1:nChunks */
+    int attempt = 0;
+    double pm;
+    for (int chunk = 1; chunk <= nchunks; ++chunk) {
+        while (k < (double)chunk * p->sel && k <= (double)p->S) {
+            int nan = 0;
+            for (size_t i = 0; i < tot; ++i) if (isnan(w->A0[i].re) || isnan(w->A0[i].im)) nan = 1;
+            if (nan) { c->stats->status |= OFX_ORACLE_STATUS_NAN; break; }
+            int kidx = (int)k - 1;                /* G33(k), 1-based */
+            double hmod = p->h * stepmod;
+            stage(c, w, w->A0, w->K1, k - 1.0, hmod, kidx);
+            for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], w->K1[i]);
+            stage(c, w, w->A1, w->K2, k - 1.0 + stepmod, hmod, kidx);
+            for (size_t i = 0; i < tot; ++i)
+                w->E[i] = cadd(cadd(w->A0[i], cscale(w->K1[i], 0.5)), cscale(w->K2[i], 0.5));
+            /* pcterr = 100 max(|Et-A1|/(|Et|+1)) over all points */
+            pm = 0.0;
+            for (size_t i = 0; i < tot; ++i) {
+                double v = 100.0 * cabs2(csub(w->E[i], w->A1[i])) / (cabs2(w->E[i]) + 1.0);
+                if (v > pm) pm = v;
+            }
+            int fl = (pm > p->maxErr ? 1 : 0) | (pm >= p->minErr ? 2 : 0);
+            fl = get_flags(c, attempt, fl);
+            c->stats->pct_max_last = pm;
+            if ((fl & 1) && stepmod > 1.0) {
+                record(c, attempt, kidx + 1, (int)stepmod, fl, 0);
+                c->stats->rejected++;
+                stepmod = stepmod - 1.0;
+            } else {
+                record(c, attempt, kidx + 1, (int)stepmod, fl, 1);
+                c->stats->accepted++;
+                c->stats->z_steps += (long long)stepmod;
+                for (int b = 0; b < c->nb; ++b) {
+                    cplx* e = w->E + (size_t)b * n;
+                    for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_nee(i, n, p->dt));
+                    fft_exec(&w->plan, e, 0);
+                    for (int i = 0; i < n; ++i) {
+                        cplx f = cscale(cexpi(-c->beta[i] * stepmod), pow(c->alpha[i], stepmod));
+                        e[i] = cmul(e[i], f);
+                    }
+                    fft_exec(&w->plan, e, 1);
+                    cplx* a0 = w->A0 + (size_t)b * n;
+                    for (int i = 0; i < n; ++i) a0[i] = cscale(e[i], 1.0 / (double)n);
+                }
+                if (!(fl & 2)) stepmod = stepmod + 1.0;     /* pcterr < minErr */
+                if (k < (double)p->S && (k + stepmod) > (double)p->S) stepmod = (double)p->S - k;
+                k = k + stepmod;
+            }
+            attempt++;
+        }
+        /* ApFT(:,chunk) = fft(Et) */
+        if (c->Ap) {
+            for (int b = 0; b < c->nb; ++b) {
+                long long off = ((long long)(c->b0 + b) * nchunks + (chunk - 1)) * (long long)n;
+                if (off >= 0 && off + n <= c->ap_len) {
+                    memcpy(c->Ap + off, w->A0 + (size_t)b * n, sizeof(cplx) * (size_t)n);
+                    fft_exec(&w->plan, c->Ap + off, 0);
+                } else c->stats->status |= OFX_ORACLE_STATUS_AP_RANGE;
+            }
+        }
+    }
+    c->stats->attempts = attempt;
+    c->stats->k_final = k;
+    c->stats->stepmod_final = stepmod;
+    c->stats->nchunks = nchunks;
+    if (c->n_attempts) *c->n_attempts = attempt;
+}
+
+static int run_schedule(sched_ctx* c) {
+    const ofx_oracle_params* p = c->p;
+    work w;
+    int time_mode = p->method == OFX_ORACLE_HEUN_NEE ? OFX_TIME_NEE : p->time_mode;
+    if (work_init(&w, p->N, c->nb, time_mode, p->w0, p->dt)) { work_free(&w); return OFX_ORACLE_ENOMEM; }
+    memcpy(w.A0, c->E_in + (size_t)c->b0 * p->N, sizeof(cplx) * (size_t)p->N * c->nb);
+    memset(c->stats, 0, sizeof(*c->stats));
+    if (p->method == OFX_ORACLE_HEUN_MEX) run_heun_mex(c, &w);
+    else if (p->method == OFX_ORACLE_RK23_MEX) run_rk23_mex(c, &w);
+    else run_heun_nee(c, &w);
+    memcpy(c->A_out + (size_t)c->b0 * p->N, w.A0, sizeof(cplx) * (size_t)p->N * c->nb);
+    work_free(&w);
+    return 0;
+}
+
+int ofx_oracle_run(const ofx_oracle_params* p,
+                   const double* E_in, const double* alpha, const double* G, const double* beta,
+                   double* A_out, double* Ap, long long ap_len_complex, double* stepmods,
+                   int* trace, int trace_cap, int* n_attempts,
+                   const int* forced_flags, int n_forced,
+                   ofx_oracle_stats* stats, int nthreads) {
+    if (!p || !E_in || !alpha || !G || !beta || !A_out || !stats) return OFX_ORACLE_EINVAL;
+    if (p->N < 4 || (p->N & (p->N - 1)) || p->B < 1 || p->S < 1 || !(p->sel > 0)) return OFX_ORACLE_EINVAL;
+    int nsched = p->shared_schedule ? 1 : p->B;
+    int nb = p->shared_schedule ? p->B : 1;
+    int rc_all = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : rc_all)
+#endif
+    for (int s = 0; s < nsched; ++s) {
+        sched_ctx c;
+        memset(&c, 0, sizeof(c));
+        c.p = p; c.b0 = s * nb; c.nb = nb;
+        c.E_in = (const cplx*)E_in; c.alpha = alpha; c.G = G; c.beta = beta;
+        c.A_out = (cplx*)A_out;
+        c.Ap = (cplx*)Ap; c.ap_len = ap_len_complex;
+        c.stepmods = stepmods ? stepmods + (p->shared_schedule ? 0 : (size_t)s * p->S) : NULL;
+        c.trace = trace ? trace + (size_t)s * 3 * (size_t)trace_cap : NULL;
+        c.trace_cap = trace_cap;
+        c.n_attempts = n_attempts ? n_attempts + s : NULL;
+        c.forced = forced_flags ? forced_flags + (p->shared_schedule ? 0 : (size_t)s * n_forced) : NULL;
+        c.n_forced = n_forced;
+        c.stats = stats + s;
+        rc_all |= run_schedule(&c);
+    }
+    return rc_all;
+}
+
+int ofx_oracle_version(void) { return 1; }

@@ -1,0 +1,53 @@
+"""The C-ABI library builds, loads and exports every symbol include/optifax.h declares (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if fn.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", fn)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"^\s*(?:int|const char\s*\*)\s+(optifax_\w+)\s*\(", src, flags=re.M)
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ["optifax_create", "optifax_destroy", "optifax_opo_mex_batch", "optifax_propagate"]:
+        assert n in names
+
+
+def test_library_exports_all_declared_symbols():
+    from optifax_gb300 import _native as nat
+    from optifax_gb300 import build
+    build.build()
+    lib = ctypes.CDLL(build.LIB)
+    for n in declared_functions():
+        assert hasattr(lib, n), n
+    assert set(nat.EXPORTS) <= set(declared_functions())
+
+
+def test_status_strings_and_null_handle():
+    from optifax_gb300 import _native as nat
+    lib = nat.load()
+    assert lib.optifax_status_string(0) == b"ok"
+    assert lib.optifax_status_string(1) == b"invalid argument"
+    assert lib.optifax_destroy(None) == 5
+    assert lib.optifax_propagate(None, None, 0, 0, 0, 0, None, None) == 5
+
+
+def test_create_without_gpu_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from optifax_gb300 import _native as nat
+    lib = nat.load()
+    h = ctypes.c_void_p()
+    assert lib.optifax_create(ctypes.byref(h), 0) == 3
