@@ -19,11 +19,13 @@
 //   the 1/N scale without leaving the SM (cluster exchange for C > 1).
 //
 // Precision: FP32 field and FFT; phases exact in 64-bit fixed point (time
-// carrier w0 t, z carrier bdiffw0 z, accumulated dispersion beta z), applied
-// through FP32 sincospif; the dispersion factor of each step is
-// conj(g(z_old)) g(z_new) with g(z) = exp(-i beta z) so that rounding of the
-// unit factors telescopes instead of accumulating; the inverse FFT applies the
-// exact reciprocal of each forward twiddle.
+// carrier w0 t, z carrier bdiffw0 z, accumulated dispersion beta z).  The
+// linear sub-step is applied as an increment, A_new = E + IFFT((D-1) FFT(E))/N,
+// with D - 1 = -2 sin^2(beta s/2) - i sin(beta s) evaluated without
+// cancellation, so transform rounding scales with |D - 1| rather than |E|; the
+// per-mode phase actually applied is tracked in fixed point and its FP32
+// rounding fed back into the next step (no drift of the accumulated phase);
+// the inverse FFT applies the exact reciprocal of each forward twiddle.
 #pragma once
 #include <cooperative_groups.h>
 #include "ofx_fft.cuh"
@@ -93,9 +95,10 @@ __device__ __forceinline__ float abc_factor(int i, int n, int mode) {
     int gi1 = 6 * (n / 16), gi2 = 10 * (n / 16);
     if (!(i > gi1 && i < gi2)) return 1.f;
     if (mode == ABC_HARD) return 0.f;
+    // 1 - sech^2(pos) evaluated as tanh^2(pos): no cancellation near the window edge
     float pos = (48.f * fabsf((float)i - 0.5f * (float)n)) / (float)n;
-    float g = coshf(pos);
-    return 1.f - 1.f / (g * g);
+    float th = tanhf(pos);
+    return th * th;
 }
 
 __device__ __forceinline__ float2 zphase(uint64_t tau_z4, float pos) {
@@ -114,8 +117,8 @@ struct Smem {
     static constexpr size_t off_buf = 0;
     static constexpr size_t off_tau = off_buf + sizeof(float2) * PADM * NBUF;
     static constexpr size_t off_l2a = off_tau + sizeof(uint64_t) * M;
-    static constexpr size_t off_gq = off_l2a + sizeof(float) * M;
-    static constexpr size_t off_edge = off_gq + sizeof(float2) * M;
+    static constexpr size_t off_papp = off_l2a + sizeof(float) * M;
+    static constexpr size_t off_edge = off_papp + sizeof(uint64_t) * M;
     static constexpr size_t off_red = off_edge + sizeof(float2) * 4 * T;
     static constexpr size_t bytes = off_red + 256;
 };
@@ -186,7 +189,8 @@ __device__ __forceinline__ void exchange_forward(const float2* bufE, float2* buf
 }
 
 // Inverse of exchange_forward: from every CTA's X buffer (local inverse
-// transforms, natural n2 order) back to the E buffers, scaled by 1/N.
+// transforms, natural n2 order), scaled by 1/N and added to the E buffers
+// (which still hold the field the increment applies to).
 template <int M, int C>
 __device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* bufE,
                                                  const Twiddle* __restrict__ twN, int t, int c, float invN) {
@@ -203,7 +207,10 @@ __device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* buf
             }
             dit_stages<N, C, C>(v, 0, twN);
 #pragma unroll
-            for (int n1 = 0; n1 < C; ++n1) remote<C>(bufE, n1)[phys(n2)] = cscale(v[n1], invN);
+            for (int n1 = 0; n1 < C; ++n1) {
+                float2* dst = remote<C>(bufE, n1) + phys(n2);
+                *dst = cadd(*dst, cscale(v[n1], invN));
+            }
         }
     }
 }
@@ -258,7 +265,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
     float2* bufK = bufX + SM::PADM;   // RK23 only: FSAL K1 (own points)
     uint64_t* tau_s = reinterpret_cast<uint64_t*>(smem + SM::off_tau);
     float* l2a_s = reinterpret_cast<float*>(smem + SM::off_l2a);
-    float2* gq_s = reinterpret_cast<float2*>(smem + SM::off_gq);
+    uint64_t* papp_s = reinterpret_cast<uint64_t*>(smem + SM::off_papp);
     float2* edge = reinterpret_cast<float2*>(smem + SM::off_edge);
     int* red = reinterpret_cast<int*>(smem + SM::off_red);
 
@@ -268,7 +275,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
     const PulseDev& P = pulses[p];
 
     // ---- prologue -------------------------------------------------------
-    if (t < 64) red[t] = 0;
+    for (int i = t; i < 64; i += T) red[i] = 0;
     float2 cph[16], a[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
@@ -282,13 +289,15 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
         int slot = 16 * t + j;
         int k = c + C * bitrev(slot, LOG2M);
         double b = (double)P.beta[k];
-        double r = b - 6.283185307179586 * rint(b * 0.15915494309189535);
-        double x = r * 2.9357677120600766e18;          // 2^64 / (2 pi)
+        constexpr double kTwoPi = 6.283185307179586476925286766559;
+        constexpr double kTurnScale = 18446744073709551616.0 / kTwoPi;   // 2^64 / (2 pi)
+        double r = b - kTwoPi * rint(b / kTwoPi);
+        double x = r * kTurnScale;
         if (x >= 9.2233720368547758e18) x -= 1.8446744073709552e19;
         if (x < -9.2233720368547758e18) x += 1.8446744073709552e19;
         tau_s[j * T + t] = (uint64_t)(long long)llrint(x);
         l2a_s[j * T + t] = log2f(P.alpha[k]);
-        gq_s[j * T + t] = make_float2(1.f, 0.f);
+        papp_s[j * T + t] = 0;
     }
     if constexpr (C > 1) cg::this_cluster().sync(); else __syncthreads();
 
@@ -358,7 +367,9 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                     }
                     if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
                     int i = c * M + 16 * t + j;
-                    bufE[phys(16 * t + j)] = cscale(e, abc_factor(i, N, cfg.abc_mode));
+                    float2 ea = cscale(e, abc_factor(i, N, cfg.abc_mode));
+                    bufE[phys(16 * t + j)] = ea;
+                    if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
                 }
             } else {
                 // ---- RK23: stage 2 (K2 at k + s/2), stage 3 (K3 at k + 3s/4), stage 4 (K4 at k + s)
@@ -400,7 +411,9 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                     }
                     if (!(isfinite(ev[j].x) && isfinite(ev[j].y))) bits |= 4;
                     int i = c * M + 16 * t + j;
-                    bufE[phys(16 * t + j)] = cscale(ev[j], abc_factor(i, N, cfg.abc_mode));
+                    float2 ea = cscale(ev[j], abc_factor(i, N, cfg.abc_mode));
+                    bufE[phys(16 * t + j)] = ea;
+                    if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
                     bufK[phys(16 * t + j)] = k4;   // FSAL candidate (own points)
                 }
             }
@@ -458,6 +471,9 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                 const unsigned qn = q + (unsigned)s_used;
 
                 // ---- linear sub-step: FFT, dispersion, inverse FFT ----
+                // Incremental form: A_new = E + IFFT((D - 1) FFT(E)) / N with
+                // D = alpha^s exp(-i beta s).  Rounding in the transforms then
+                // scales with |D - 1| instead of |E|.
                 float2* fbuf = (C > 1) ? bufX : bufE;
                 if constexpr (C > 1) {
                     exchange_forward<M, C>(bufE, bufX, twN, t, c);
@@ -470,14 +486,28 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                 float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    uint64_t ph = tau_s[j * T + t] * (uint64_t)qn;
-                    float2 gn = turn_to_unit((uint64_t)0 - ph);
-                    float2 go = gq_s[j * T + t];
-                    float amp = exp2f((float)s_used * l2a_s[j * T + t]);
-                    float2 f = cmulc(gn, go);
-                    v[j] = cscale(cmul(v[j], f), amp);
-                    gq_s[j * T + t] = gn;
-                    if (apc) apc[c + C * bitrev(16 * t + j, LOG2M)] = v[j];
+                    // phase increment beta*s from the exact fixed-point target minus the
+                    // phase applied so far (error feedback: FP32 rounding of the
+                    // increment is carried into the next step instead of accumulating)
+                    uint64_t target = tau_s[j * T + t] * (uint64_t)qn;
+                    uint64_t papp = papp_s[j * T + t];
+                    long long dfix = (long long)(target - papp);
+                    float df = (float)dfix;                       // units of 2^-64 turn
+                    if (df >= 0x1p63f) df = 0x1.fffffep62f;
+                    papp_s[j * T + t] = papp + (uint64_t)(long long)df;
+                    float s2, c2;
+                    sincospif(df * 0x1p-64f, &s2, &c2);           // sin, cos of (beta s)/2
+                    float2 dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);   // exp(-i beta s) - 1
+                    float l2 = l2a_s[j * T + t];
+                    if (l2 != 0.f) {
+                        float x = (float)s_used * l2;
+                        float as = exp2f(x);
+                        float am1 = expm1f(x * 0.69314718055994531f);
+                        dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
+                    }
+                    float2 eh = v[j];
+                    if (apc) apc[c + C * bitrev(16 * t + j, LOG2M)] = cadd(eh, cmul(eh, dm1));
+                    v[j] = cmul(eh, dm1);
                 }
                 fft_inverse_from_regs<M>(fbuf, twM, t, v);
                 if constexpr (C > 1) {
@@ -488,7 +518,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                     for (int j = 0; j < 16; ++j) a[j] = bufE[phys(16 * t + j)];
                 } else {
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) a[j] = cscale(bufE[phys(16 * t + j)], invN);
+                    for (int j = 0; j < 16; ++j)
+                        a[j] = cadd(bufX[phys(16 * t + j)], cscale(bufE[phys(16 * t + j)], invN));
                 }
                 if constexpr (METHOD == OPTIFAX_RK23) {
 #pragma unroll
