@@ -66,7 +66,16 @@ typedef struct {
     float stepmod_final;
     int32_t n_chunks;
     int32_t reserved[3];
-} optifax_pulse_stats;
+} optifax_pulse_stats;   /* reserved[0]: round trips completed */
+
+/* Per round trip of a synchronously pumped OPO. */
+typedef struct {
+    int32_t attempts;
+    int32_t accepted;
+    int32_t rejected;
+    int32_t status;         /* OPTIFAX_PULSE_* bits of this trip */
+    double tally[4];        /* sum_k tally_w[i][k] |X_k|^2 of the crystal-output spectrum, FP64 */
+} optifax_trip_record;
 
 /* One crystal pass of one pulse (all pointers are device pointers). */
 typedef struct {
@@ -92,6 +101,34 @@ typedef struct {
     float sel;               /* steps per progress chunk */
     int32_t stepmods_limit;  /* stepmods recorded for k < limit (0: the variant's own rule) */
 } optifax_pulse;
+
+/*
+ * A synchronously pumped OPO cavity (reference: OpticalSim.run,
+ * toolbox/lib/classes/OpticalSim.m:207-301; per-trip optics
+ * OpticalPulse.m:137-197,256-261,518-527; Cavity.m:50-87).  Every round trip
+ * runs one crystal pass of `pass`; the crystal-output spectrum X (natural FFT
+ * order of the fftshifted field) then becomes the next crystal input
+ *     Y_k = X_k feedback[k] + pump[k],
+ * where feedback folds the refraction out of and back into the crystal, the
+ * intracavity optics, the output coupler's intracavity share and the delay,
+ * and pump is the in-crystal pump spectrum.  pass.E_in is the first trip's
+ * crystal input; pass.A_out receives the crystal input of the trip after the
+ * last one (so a run resumes by passing it back as E_in).  All pointers are
+ * device pointers.
+ */
+typedef struct {
+    optifax_pulse pass;
+    const void* feedback;        /* N complex, natural FFT order */
+    const void* pump;            /* N complex, natural FFT order */
+    const float* tally_w;        /* n_tally x N energy weights (may be NULL if n_tally == 0) */
+    optifax_trip_record* trips;  /* n_trips records (optional) */
+    int32_t n_trips;
+    int32_t n_tally;             /* 0..4 */
+    int32_t steady_trips;        /* stop after this many consecutive flat trips (0: never) */
+    int32_t steady_tally;        /* tally index tested for flatness */
+    float steady_tol;            /* |T_n - T_{n-1}| <= tol |T_n| counts as flat */
+    int32_t reserved;
+} optifax_opo;
 
 /* Create / destroy a context on a CUDA device.  The context owns the twiddle
  * tables and the pulse-descriptor staging buffers (device workspace). */
@@ -137,6 +174,15 @@ int optifax_opo_mex_batch(optifax_handle h,
 int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
                       int32_t method, int32_t variant, int32_t cta_points,
                       optifax_pulse_stats* stats, void* stream);
+
+/*
+ * Run n_cavities independent OPO cavities (e.g. delay scans, replicas) for
+ * their round trips in one launch, Heun schedule with the given variant's
+ * conventions.  stats (optional, device): per-cavity totals, reserved[0] =
+ * trips completed (fewer than n_trips when the steady-state test stopped it).
+ */
+int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cavities,
+                    int32_t variant, int32_t cta_points, optifax_pulse_stats* stats, void* stream);
 
 #ifdef __cplusplus
 }

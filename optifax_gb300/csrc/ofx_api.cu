@@ -318,6 +318,51 @@ int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_p
     return OPTIFAX_OK;
 }
 
+int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cavities,
+                    int32_t variant, int32_t cta_points, optifax_pulse_stats* stats, void* stream) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!cavities || n_cavities < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "no cavities");
+    VariantCfg vc;
+    if (!variant_cfg(variant, &vc)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown variant");
+    if (cta_points != 0 && (!is_pow2(cta_points) || cta_points < 512 || cta_points > 4096))
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "cta_points must be 0 or a power of two in [512, 4096]");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    std::map<std::pair<int, int>, std::vector<PulseDev>> groups;
+    for (int i = 0; i < n_cavities; ++i) {
+        const optifax_opo& cv = cavities[i];
+        if (!cv.feedback || !cv.pump) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "feedback and pump are required");
+        if (cv.n_trips < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_trips must be >= 1");
+        if (cv.n_tally < 0 || cv.n_tally > 4 || (cv.n_tally > 0 && !cv.tally_w))
+            return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_tally must be 0..4 with tally_w");
+        if (cv.steady_trips < 0 || cv.steady_tally < 0 || cv.steady_tally >= 4)
+            return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "bad steady-state settings");
+        PulseDev d;
+        int rc = fill_desc(h, cv.pass, vc, &d, stats ? stats + i : nullptr);
+        if (rc) return rc;
+        d.fb = (const float2*)cv.feedback;
+        d.pump = (const float2*)cv.pump;
+        d.tally_w = cv.tally_w;
+        d.trips = cv.trips;
+        d.n_trips = cv.n_trips;
+        d.n_tally = cv.n_tally;
+        d.steady_trips = cv.steady_trips;
+        d.steady_tally = cv.steady_tally;
+        d.steady_tol = cv.steady_tol;
+        int M = choose_M(cv.pass.n_points, cta_points);
+        if (M > cv.pass.n_points) M = cv.pass.n_points;
+        int C = cv.pass.n_points / M;
+        if (C > 16) return fail(h, OPTIFAX_ERR_UNSUPPORTED, "n_points / cta_points exceeds 16");
+        groups[{M, C}].push_back(d);
+    }
+    for (auto& g : groups) {
+        int rc = launch_group(h, g.second, g.first.first, g.first.second, OPTIFAX_HEUN, vc, false,
+                              (cudaStream_t)stream);
+        if (rc) return rc;
+    }
+    return OPTIFAX_OK;
+}
+
 int optifax_opo_mex_batch(optifax_handle h,
                           const void* E, const float* alpha_w, const float* G,
                           float w0, double bdiffw0, float step_h, int32_t n_steps, double dt,

@@ -54,6 +54,13 @@ struct PulseDev {
     uint64_t tau_z4;         // bdiffw0 h / 4 in turns (fixed point), per quarter step
     float w0, h, max_err, min_err, sel, c_shock;
     int N, S, nchunks, stepmods_limit, trace_cap, n_forced;
+    // synchronously pumped OPO (fb != nullptr): per-mode round-trip transfer
+    const float2* fb;        // crystal-output spectrum -> next crystal-input spectrum
+    const float2* pump;      // pump spectrum added at the crystal input each trip
+    const float* tally_w;    // n_tally x N energy weights on the crystal-output spectrum
+    optifax_trip_record* trips;
+    int n_trips, n_tally, steady_trips, steady_tally;
+    float steady_tol;
 };
 
 struct KernelCfg {
@@ -120,7 +127,8 @@ struct Smem {
     static constexpr size_t off_papp = off_l2a + sizeof(float) * M;
     static constexpr size_t off_edge = off_papp + sizeof(uint64_t) * M;
     static constexpr size_t off_red = off_edge + sizeof(float2) * 4 * T;
-    static constexpr size_t bytes = off_red + 256;
+    static constexpr size_t off_dred = off_red + 256;               // FP64 reduction slots
+    static constexpr size_t bytes = off_dred + sizeof(double) * (8 * 4 + 2 * 16 * 4 + 4);
 };
 
 // ---------------------------------------------------------------------------
@@ -189,11 +197,12 @@ __device__ __forceinline__ void exchange_forward(const float2* bufE, float2* buf
 }
 
 // Inverse of exchange_forward: from every CTA's X buffer (local inverse
-// transforms, natural n2 order), scaled by 1/N and added to the E buffers
-// (which still hold the field the increment applies to).
+// transforms, natural n2 order), scaled by 1/N and either added to the E
+// buffers (which still hold the field an increment applies to) or stored.
 template <int M, int C>
 __device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* bufE,
-                                                 const Twiddle* __restrict__ twN, int t, int c, float invN) {
+                                                 const Twiddle* __restrict__ twN, int t, int c, float invN,
+                                                 bool accumulate) {
     if constexpr (C > 1) {
         constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
 #pragma unroll
@@ -209,7 +218,7 @@ __device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* buf
 #pragma unroll
             for (int n1 = 0; n1 < C; ++n1) {
                 float2* dst = remote<C>(bufE, n1) + phys(n2);
-                *dst = cadd(*dst, cscale(v[n1], invN));
+                *dst = accumulate ? cadd(*dst, cscale(v[n1], invN)) : cscale(v[n1], invN);
             }
         }
     }
@@ -249,8 +258,54 @@ __device__ __forceinline__ int reduce_flags(int bits, int* red, int attempt, int
 }
 
 // ---------------------------------------------------------------------------
+// FP64 sum of 4 per-thread values over the CTA and the cluster; every thread
+// of every CTA returns the same totals (ranks summed in a fixed order).
+// ---------------------------------------------------------------------------
+template <int M, int C>
+__device__ __forceinline__ void reduce_tallies(const float (&part)[4], double (&out)[4], double* dred,
+                                               int t, int c, int parity) {
+    constexpr int T = M / 16, NW = T / 32;
+    double v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v[i] = (double)part[i];
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    }
+    if ((t & 31) == 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) dred[(t >> 5) * 4 + i] = v[i];
+    }
+    __syncthreads();
+    double* cl = dred + 8 * 4 + parity * 16 * 4;
+    if (t == 0) {
+        double s[4] = {0, 0, 0, 0};
+        for (int w = 0; w < NW; ++w)
+            for (int i = 0; i < 4; ++i) s[i] += dred[w * 4 + i];
+        for (int r = 0; r < C; ++r) {
+            double* dst = remote<C>(cl, r) + c * 4;
+            for (int i = 0; i < 4; ++i) dst[i] = s[i];
+        }
+    }
+    csync<C>();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        double s = 0.0;
+        for (int r = 0; r < C; ++r) s += cl[r * 4 + i];
+        out[i] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // the kernel
 // ---------------------------------------------------------------------------
+// One launch runs n_trips crystal passes of every pulse.  With a round-trip
+// transfer (OPO mode, reference OpticalSim.run, OpticalSim.m:230-288) the last
+// accepted step of each pass maps its spectrum X through the cavity,
+// Y = X fb + pump, and the next pass starts from IFFT(Y): refraction into
+// and out of the crystal, the intracavity optics, the output coupler, the
+// delay and the pump injection are all per-mode products folded into fb and
+// pump by the host.  Per-trip energy tallies sum tally_w |X|^2 in FP64.
 template <int M, int C, int METHOD>
 __global__ void __launch_bounds__(M / 16, 1)
 pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM,
@@ -268,6 +323,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
     uint64_t* papp_s = reinterpret_cast<uint64_t*>(smem + SM::off_papp);
     float2* edge = reinterpret_cast<float2*>(smem + SM::off_edge);
     int* red = reinterpret_cast<int*>(smem + SM::off_red);
+    double* dred = reinterpret_cast<double*>(smem + SM::off_dred);
 
     const int t = threadIdx.x;
     const int c = (C > 1) ? (int)cg::this_cluster().block_rank() : 0;
@@ -297,7 +353,6 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
         if (x < -9.2233720368547758e18) x += 1.8446744073709552e19;
         tau_s[j * T + t] = (uint64_t)(long long)llrint(x);
         l2a_s[j * T + t] = log2f(P.alpha[k]);
-        papp_s[j * T + t] = 0;
     }
     if constexpr (C > 1) cg::this_cluster().sync(); else __syncthreads();
 
@@ -307,228 +362,279 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
     const float invN = 1.0f / (float)N;
     const int guard = cfg.guard;
     const long long max_attempts = (long long)cfg.max_attempts_mul * (long long)(P.S + 16) + 64;
+    const int nchunks = P.nchunks;
+    const float pass_end = (float)nchunks * sel;
+    const bool opo = P.fb != nullptr;
+    const int n_trips = P.n_trips > 0 ? P.n_trips : 1;
+    const bool rec = (c == 0 && t == 0);
 
     float k = 0.f, stepprev = 4.f, stepmod = 4.f;
     unsigned q = 0;                          // accumulated dispersion position (sum of stepmod)
-    int attempt = 0, n_acc = 0, n_rej = 0, status = 0, par = 0;
-    const bool rec = (c == 0 && t == 0);
+    int attempt = 0, n_acc = 0, n_rej = 0, status = 0, par = 0, trip = 0, trips_done = 0;
+    int gatt = 0, tot_att = 0, tot_acc = 0, tot_rej = 0, steady_count = 0;
+    double prev_tally = 0.0;
 
-    // RK23 carries K1 (first stage, FSAL) between attempts in registers
-    float2 k1r[16];
-    if constexpr (METHOD == OPTIFAX_RK23) {
-        // initial K1 at k = 0 with stepmod = 4 (OPO_CUDA_ODE23.cu:432-438)
-        float hg = (stepmod * h) * G[0];
-        float2 z = zphase(P.tau_z4, 0.f);
-        float2 nl[16];
+    float2 k1r[16];   // RK23: K1 (first stage, FSAL) between attempts
+    for (trip = 0; trip < n_trips; ++trip) {
+        k = 0.f; stepprev = 4.f; stepmod = 4.f; q = 0;
+        attempt = 0; n_acc = 0; n_rej = 0;
+        int trip_status = 0;
+        double tally[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 1
+        for (int j = 0; j < 16; ++j) papp_s[j * T + t] = 0;
+        if constexpr (METHOD == OPTIFAX_RK23) {
+            // initial K1 at k = 0 with stepmod = 4 (OPO_CUDA_ODE23.cu:432-438)
+            float hg = (stepmod * h) * G[0];
+            float2 z = zphase(P.tau_z4, 0.f);
+            float2 nl[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
-        float2 L, R;
-        exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+            for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
+            float2 L, R;
+            exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-            k1r[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-    }
+            for (int j = 0; j < 16; ++j)
+                k1r[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+        }
 
-    const int nchunks = P.nchunks;
-    for (int chunk = 0; chunk < nchunks; ++chunk) {
-        stepmod = stepprev;
-        const float cend = (float)(chunk + 1) * sel;
-        while (k < cend && (!guard || k < Sf)) {
-            if (attempt >= max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; goto done; }
-            const int kidx = (int)k;
-            const float hmod = stepmod * h;
-            const float hg = hmod * G[kidx];
-            int bits = 0;
-            if constexpr (METHOD == OPTIFAX_HEUN) {
-                // ---- stage 1: K1 = f(A0) at z = k ----
-                float2 nl[16], k1[16], L, R;
-                float2 z = zphase(P.tau_z4, k);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
-                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
-#pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    k1[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-                // ---- stage 2: K2 = f(A0 + K1) at z = k + stepmod ----
-                z = zphase(P.tau_z4, k + stepmod);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], k1[j]), cph[j], z);
-                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float2 k2 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-                    float2 e = cadd(a[j], cadd(cscale(k2, 0.5f), cscale(k1[j], 0.5f)));
-                    float2 d = cscale(csub(k2, k1[j]), 0.5f);          // = E - A1
-                    float ae = cabsf2(e);
-                    if (ae > 0.f) {
-                        float pct = 100.f * (cabsf2(d) / (ae + 1.f));
-                        if (pct >= maxE) bits |= 1;
-                        else if (pct >= minE) bits |= 2;
-                    }
-                    if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
-                    int i = c * M + 16 * t + j;
-                    float2 ea = cscale(e, abc_factor(i, N, cfg.abc_mode));
-                    bufE[phys(16 * t + j)] = ea;
-                    if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
-                }
-            } else {
-                // ---- RK23: stage 2 (K2 at k + s/2), stage 3 (K3 at k + 3s/4), stage 4 (K4 at k + s)
-                float2 nl[16], k2[16], pp[16], L, R;
-                float2 z = zphase(P.tau_z4, k + 0.5f * stepmod);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], cscale(k1r[j], 0.5f)), cph[j], z);
-                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
-#pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    k2[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-                z = zphase(P.tau_z4, k + 0.75f * stepmod);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], cscale(k2[j], 0.75f)), cph[j], z);
-                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
-                float2 ev[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float2 k3 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-                    float2 e = cadd(a[j], cadd(cscale(k3, 4.f / 9.f), cscale(k2[j], 1.f / 3.f)));
-                    ev[j] = cadd(e, cscale(k1r[j], 2.f / 9.f));
-                    // E - A1 without K4: (4/9-1/3) K3 + (1/3-1/4) K2 + (2/9-7/24) K1
-                    pp[j] = cadd(cadd(cscale(k3, 1.f / 9.f), cscale(k2[j], 1.f / 12.f)),
-                                 cscale(k1r[j], -5.f / 72.f));
-                }
-                z = zphase(P.tau_z4, k + stepmod);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) nl[j] = nl_eval(ev[j], cph[j], z);
-                exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float2 k4 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-                    float2 d = csub(pp[j], cscale(k4, 1.f / 8.f));  // = E - A1
-                    float ae = cabsf2(ev[j]);
-                    if (ae > 0.f) {
-                        float pct = 200.f * (cabsf2(d) / (ae + 1.f));
-                        if (pct >= maxE) bits |= 1;
-                        else if (pct >= minE) bits |= 2;
-                    }
-                    if (!(isfinite(ev[j].x) && isfinite(ev[j].y))) bits |= 4;
-                    int i = c * M + 16 * t + j;
-                    float2 ea = cscale(ev[j], abc_factor(i, N, cfg.abc_mode));
-                    bufE[phys(16 * t + j)] = ea;
-                    if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
-                    bufK[phys(16 * t + j)] = k4;   // FSAL candidate (own points)
-                }
-            }
-
-            int fl = reduce_flags<M, C>(bits, red, attempt, t, c, cfg);
-            if (P.forced && attempt < P.n_forced) fl = (P.forced[attempt] & 3) | (fl & 4);
-            if (fl & 4) status |= OPTIFAX_PULSE_NAN;
-
-            if ((fl & 1) && stepmod > 1.f && (k - stepmod) > 0.f) {
-                // ---- reject: A0 unchanged; k moves back by one in net (the loop adds the new stepmod)
-                if (rec && P.trace && attempt < P.trace_cap) {
-                    P.trace[3 * attempt] = kidx; P.trace[3 * attempt + 1] = (int)stepmod;
-                    P.trace[3 * attempt + 2] = fl & 7;
-                }
-                ++n_rej;
-                k = k - stepmod;
-                stepmod = stepmod - 1.f;
-                stepprev = stepmod;
-                if constexpr (METHOD == OPTIFAX_RK23) {
-                    // K1 recomputed at z = k + stepmod with G[k] (OPO_CUDA_ODE23.cu:484-487)
-                    float hg1 = (stepmod * h) * G[(int)k];
-                    float2 z = zphase(P.tau_z4, k + stepmod);
-                    float2 nl[16], L, R;
+        for (int chunk = 0; chunk < nchunks; ++chunk) {
+            stepmod = stepprev;
+            const float cend = (float)(chunk + 1) * sel;
+            while (k < cend && (!guard || k < Sf)) {
+                if (attempt >= max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; goto done; }
+                const int kidx = (int)k;
+                const float hmod = stepmod * h;
+                const float hg = hmod * G[kidx];
+                int bits = 0;
+                if constexpr (METHOD == OPTIFAX_HEUN) {
+                    // ---- stage 1: K1 = f(A0) at z = k ----
+                    float2 nl[16], k1[16], L, R;
+                    float2 z = zphase(P.tau_z4, k);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
                     exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
 #pragma unroll
                     for (int j = 0; j < 16; ++j)
-                        k1r[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg1, cs);
-                }
-            } else {
-                // ---- accept ----
-                if (rec && P.trace && attempt < P.trace_cap) {
-                    P.trace[3 * attempt] = kidx; P.trace[3 * attempt + 1] = (int)stepmod;
-                    P.trace[3 * attempt + 2] = (fl & 7) | 8;
-                }
-                ++n_acc;
-                const int s_used = (int)stepmod;
-                if (rec && P.stepmods && kidx < P.stepmods_limit && kidx < P.S) P.stepmods[kidx] = (float)s_used;
-                // step control (OPO_CUDA_BATCH_XTAL.cu:487-506; ODE23 :519-538 doubles)
-                if (k + stepmod >= cend && k < cend - 1.f) {
-                    float stepend = (cend - k) - 1.f;
-                    stepprev = stepmod;
-                    stepmod = stepend;
-                } else {
-                    if constexpr (METHOD == OPTIFAX_HEUN) {
-                        if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.f) < cend - 1.f) stepmod = stepmod + 1.f;
-                    } else {
-                        if (!(fl & 2) && !(fl & 1) && (k + stepmod + stepmod) < cend - 1.f) stepmod = stepmod * 2.f;
-                    }
-                    stepprev = stepmod;
-                }
-                const float knext = k + stepmod;
-                const bool last_in_chunk = !(knext < cend && (!guard || knext < Sf));
-                const unsigned qn = q + (unsigned)s_used;
-
-                // ---- linear sub-step: FFT, dispersion, inverse FFT ----
-                // Incremental form: A_new = E + IFFT((D - 1) FFT(E)) / N with
-                // D = alpha^s exp(-i beta s).  Rounding in the transforms then
-                // scales with |D - 1| instead of |E|.
-                float2* fbuf = (C > 1) ? bufX : bufE;
-                if constexpr (C > 1) {
-                    exchange_forward<M, C>(bufE, bufX, twN, t, c);
-                    cg::this_cluster().sync();
-                } else {
-                    __syncthreads();
-                }
-                float2 v[16];
-                fft_forward_to_regs<M>(fbuf, twM, t, v);
-                float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
+                        k1[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                    // ---- stage 2: K2 = f(A0 + K1) at z = k + stepmod ----
+                    z = zphase(P.tau_z4, k + stepmod);
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    // phase increment beta*s from the exact fixed-point target minus the
-                    // phase applied so far (error feedback: FP32 rounding of the
-                    // increment is carried into the next step instead of accumulating)
-                    uint64_t target = tau_s[j * T + t] * (uint64_t)qn;
-                    uint64_t papp = papp_s[j * T + t];
-                    long long dfix = (long long)(target - papp);
-                    float df = (float)dfix;                       // units of 2^-64 turn
-                    if (df >= 0x1p63f) df = 0x1.fffffep62f;
-                    papp_s[j * T + t] = papp + (uint64_t)(long long)df;
-                    float s2, c2;
-                    sincospif(df * 0x1p-64f, &s2, &c2);           // sin, cos of (beta s)/2
-                    float2 dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);   // exp(-i beta s) - 1
-                    float l2 = l2a_s[j * T + t];
-                    if (l2 != 0.f) {
-                        float x = (float)s_used * l2;
-                        float as = exp2f(x);
-                        float am1 = expm1f(x * 0.69314718055994531f);
-                        dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
-                    }
-                    float2 eh = v[j];
-                    if (apc) apc[c + C * bitrev(16 * t + j, LOG2M)] = cadd(eh, cmul(eh, dm1));
-                    v[j] = cmul(eh, dm1);
-                }
-                fft_inverse_from_regs<M>(fbuf, twM, t, v);
-                if constexpr (C > 1) {
-                    cg::this_cluster().sync();
-                    exchange_inverse<M, C>(bufX, bufE, twN, t, c, invN);
-                    cg::this_cluster().sync();
+                    for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], k1[j]), cph[j], z);
+                    exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) a[j] = bufE[phys(16 * t + j)];
+                    for (int j = 0; j < 16; ++j) {
+                        float2 k2 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                        float2 e = cadd(a[j], cadd(cscale(k2, 0.5f), cscale(k1[j], 0.5f)));
+                        float2 d = cscale(csub(k2, k1[j]), 0.5f);          // = E - A1
+                        float ae = cabsf2(e);
+                        if (ae > 0.f) {
+                            float pct = 100.f * (cabsf2(d) / (ae + 1.f));
+                            if (pct >= maxE) bits |= 1;
+                            else if (pct >= minE) bits |= 2;
+                        }
+                        if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
+                        int i = c * M + 16 * t + j;
+                        float2 ea = cscale(e, abc_factor(i, N, cfg.abc_mode));
+                        bufE[phys(16 * t + j)] = ea;
+                        if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
+                    }
                 } else {
+                    // ---- RK23: K2 at k + s/2, K3 at k + 3s/4, K4 at k + s (FSAL) ----
+                    float2 nl[16], k2[16], pp[16], L, R;
+                    float2 z = zphase(P.tau_z4, k + 0.5f * stepmod);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], cscale(k1r[j], 0.5f)), cph[j], z);
+                    exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
 #pragma unroll
                     for (int j = 0; j < 16; ++j)
-                        a[j] = cadd(bufX[phys(16 * t + j)], cscale(bufE[phys(16 * t + j)], invN));
-                }
-                if constexpr (METHOD == OPTIFAX_RK23) {
+                        k2[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                    z = zphase(P.tau_z4, k + 0.75f * stepmod);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) k1r[j] = bufK[phys(16 * t + j)];
+                    for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], cscale(k2[j], 0.75f)), cph[j], z);
+                    exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+                    float2 ev[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        float2 k3 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                        float2 e = cadd(a[j], cadd(cscale(k3, 4.f / 9.f), cscale(k2[j], 1.f / 3.f)));
+                        ev[j] = cadd(e, cscale(k1r[j], 2.f / 9.f));
+                        // E - A1 without K4: (4/9-1/3) K3 + (1/3-1/4) K2 + (2/9-7/24) K1
+                        pp[j] = cadd(cadd(cscale(k3, 1.f / 9.f), cscale(k2[j], 1.f / 12.f)),
+                                     cscale(k1r[j], -5.f / 72.f));
+                    }
+                    z = zphase(P.tau_z4, k + stepmod);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) nl[j] = nl_eval(ev[j], cph[j], z);
+                    exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        float2 k4 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
+                        float2 d = csub(pp[j], cscale(k4, 1.f / 8.f));  // = E - A1
+                        float ae = cabsf2(ev[j]);
+                        if (ae > 0.f) {
+                            float pct = 200.f * (cabsf2(d) / (ae + 1.f));
+                            if (pct >= maxE) bits |= 1;
+                            else if (pct >= minE) bits |= 2;
+                        }
+                        if (!(isfinite(ev[j].x) && isfinite(ev[j].y))) bits |= 4;
+                        int i = c * M + 16 * t + j;
+                        float2 ea = cscale(ev[j], abc_factor(i, N, cfg.abc_mode));
+                        bufE[phys(16 * t + j)] = ea;
+                        if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
+                        bufK[phys(16 * t + j)] = k4;   // FSAL candidate (own points)
+                    }
                 }
-                q = qn;
+
+                int fl = reduce_flags<M, C>(bits, red, gatt, t, c, cfg);
+                if (P.forced && gatt < P.n_forced) fl = (P.forced[gatt] & 3) | (fl & 4);
+                if (fl & 4) trip_status |= OPTIFAX_PULSE_NAN;
+
+                if ((fl & 1) && stepmod > 1.f && (k - stepmod) > 0.f) {
+                    // ---- reject: A0 unchanged; k moves back by one in net (the loop adds the new stepmod)
+                    if (rec && P.trace && gatt < P.trace_cap) {
+                        P.trace[3 * gatt] = kidx; P.trace[3 * gatt + 1] = (int)stepmod;
+                        P.trace[3 * gatt + 2] = fl & 7;
+                    }
+                    ++n_rej;
+                    k = k - stepmod;
+                    stepmod = stepmod - 1.f;
+                    stepprev = stepmod;
+                    if constexpr (METHOD == OPTIFAX_RK23) {
+                        // K1 recomputed at z = k + stepmod with G[k] (OPO_CUDA_ODE23.cu:484-487)
+                        float hg1 = (stepmod * h) * G[(int)k];
+                        float2 z = zphase(P.tau_z4, k + stepmod);
+                        float2 nl[16], L, R;
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
+                        exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            k1r[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg1, cs);
+                    }
+                } else {
+                    // ---- accept ----
+                    if (rec && P.trace && gatt < P.trace_cap) {
+                        P.trace[3 * gatt] = kidx; P.trace[3 * gatt + 1] = (int)stepmod;
+                        P.trace[3 * gatt + 2] = (fl & 7) | 8;
+                    }
+                    ++n_acc;
+                    const int s_used = (int)stepmod;
+                    if (rec && P.stepmods && kidx < P.stepmods_limit && kidx < P.S) P.stepmods[kidx] = (float)s_used;
+                    // step control (OPO_CUDA_BATCH_XTAL.cu:487-506; ODE23 :519-538 doubles)
+                    if (k + stepmod >= cend && k < cend - 1.f) {
+                        float stepend = (cend - k) - 1.f;
+                        stepprev = stepmod;
+                        stepmod = stepend;
+                    } else {
+                        if constexpr (METHOD == OPTIFAX_HEUN) {
+                            if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.f) < cend - 1.f) stepmod = stepmod + 1.f;
+                        } else {
+                            if (!(fl & 2) && !(fl & 1) && (k + stepmod + stepmod) < cend - 1.f) stepmod = stepmod * 2.f;
+                        }
+                        stepprev = stepmod;
+                    }
+                    const float knext = k + stepmod;
+                    const bool last_in_chunk = !(knext < cend && (!guard || knext < Sf));
+                    const bool pass_ends = !(knext < pass_end && (!guard || knext < Sf));
+                    const bool cav = opo && pass_ends;
+                    const unsigned qn = q + (unsigned)s_used;
+
+                    // ---- linear sub-step ----
+                    // Incremental form: A_new = E + IFFT((D - 1) FFT(E)) / N with
+                    // D = alpha^s exp(-i beta s): transform rounding then scales with
+                    // |D - 1| instead of |E|.  At the end of an OPO pass the full
+                    // spectrum goes through the cavity instead: A_new = IFFT(D FFT(E) fb + pump) / N.
+                    float2* fbuf = (C > 1) ? bufX : bufE;
+                    if constexpr (C > 1) {
+                        exchange_forward<M, C>(bufE, bufX, twN, t, c);
+                        cg::this_cluster().sync();
+                    } else {
+                        __syncthreads();
+                    }
+                    float2 v[16];
+                    fft_forward_to_regs<M>(fbuf, twM, t, v);
+                    float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
+                    float part[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        // phase increment beta*s from the exact fixed-point target minus the
+                        // phase applied so far (error feedback: FP32 rounding of the
+                        // increment is carried into the next step instead of accumulating)
+                        uint64_t target = tau_s[j * T + t] * (uint64_t)qn;
+                        uint64_t papp = papp_s[j * T + t];
+                        long long dfix = (long long)(target - papp);
+                        float df = (float)dfix;                       // units of 2^-64 turn
+                        if (df >= 0x1p63f) df = 0x1.fffffep62f;
+                        papp_s[j * T + t] = papp + (uint64_t)(long long)df;
+                        float s2, c2;
+                        sincospif(df * 0x1p-64f, &s2, &c2);           // sin, cos of (beta s)/2
+                        float2 dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);   // exp(-i beta s) - 1
+                        float l2 = l2a_s[j * T + t];
+                        if (l2 != 0.f) {
+                            float x = (float)s_used * l2;
+                            float as = exp2f(x);
+                            float am1 = expm1f(x * 0.69314718055994531f);
+                            dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
+                        }
+                        float2 eh = v[j];
+                        int kk = c + C * bitrev(16 * t + j, LOG2M);
+                        if (apc) apc[kk] = cadd(eh, cmul(eh, dm1));
+                        if (cav) {
+                            float2 X = cadd(eh, cmul(eh, dm1));
+                            float x2 = X.x * X.x + X.y * X.y;
+#pragma unroll
+                            for (int i = 0; i < 4; ++i)
+                                if (i < P.n_tally) part[i] = fmaf(P.tally_w[(size_t)i * N + kk], x2, part[i]);
+                            v[j] = cadd(cmul(X, P.fb[kk]), P.pump[kk]);
+                        } else {
+                            v[j] = cmul(eh, dm1);
+                        }
+                    }
+                    fft_inverse_from_regs<M>(fbuf, twM, t, v);
+                    if constexpr (C > 1) {
+                        cg::this_cluster().sync();
+                        exchange_inverse<M, C>(bufX, bufE, twN, t, c, invN, !cav);
+                        cg::this_cluster().sync();
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) a[j] = bufE[phys(16 * t + j)];
+                    } else {
+                        if (cav) {
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) a[j] = cscale(bufE[phys(16 * t + j)], invN);
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 16; ++j)
+                                a[j] = cadd(bufX[phys(16 * t + j)], cscale(bufE[phys(16 * t + j)], invN));
+                        }
+                    }
+                    if constexpr (METHOD == OPTIFAX_RK23) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) k1r[j] = bufK[phys(16 * t + j)];
+                    }
+                    if (cav) reduce_tallies<M, C>(part, tally, dred, t, c, trip & 1);
+                    q = qn;
+                }
+                ++attempt;
+                ++gatt;
+                k = k + stepmod;
             }
-            ++attempt;
-            k = k + stepmod;
+        }
+        status |= trip_status;
+        tot_att += attempt; tot_acc += n_acc; tot_rej += n_rej;
+        trips_done = trip + 1;
+        if (opo) {
+            if (rec && P.trips) {
+                optifax_trip_record tr;
+                tr.attempts = attempt; tr.accepted = n_acc; tr.rejected = n_rej; tr.status = trip_status;
+                for (int i = 0; i < 4; ++i) tr.tally[i] = tally[i];
+                P.trips[trip] = tr;
+            }
+            if (P.steady_trips > 0) {
+                double cur = tally[P.steady_tally & 3];
+                bool flat = trip > 0 && cur != 0.0 && fabs(cur - prev_tally) <= (double)P.steady_tol * fabs(cur);
+                steady_count = flat ? steady_count + 1 : 0;
+                prev_tally = cur;
+                if (steady_count >= P.steady_trips) break;
+            }
         }
     }
 done:
@@ -536,9 +642,9 @@ done:
     for (int j = 0; j < 16; ++j) P.A_out[c * M + 16 * t + j] = a[j];
     if (rec && P.stats) {
         optifax_pulse_stats st;
-        st.attempts = attempt; st.accepted = n_acc; st.rejected = n_rej; st.status = status;
+        st.attempts = tot_att; st.accepted = tot_acc; st.rejected = tot_rej; st.status = status;
         st.z_steps = (long long)q; st.k_final = k; st.stepmod_final = stepmod; st.n_chunks = nchunks;
-        st.reserved[0] = st.reserved[1] = st.reserved[2] = 0;
+        st.reserved[0] = trips_done; st.reserved[1] = st.reserved[2] = 0;
         *P.stats = st;
     }
 }
