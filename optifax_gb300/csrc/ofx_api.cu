@@ -22,8 +22,11 @@ using namespace ofx;
 struct optifax_context {
     int device = 0;
     std::map<int, Twiddle*> tw;          // n -> n/2 entries, W_n^e
+    std::map<int, Twiddle*> passtw;      // M -> pass-1 table [16][M/16] then pass-2 [16][M/256]
     PulseDev* d_desc = nullptr;
     size_t desc_cap = 0;
+    float2* d_xch = nullptr;             // cluster exchange scratch
+    size_t xch_cap = 0;                  // in complex values
     int* d_grid_flags = nullptr;
     std::string last_error;
 };
@@ -40,6 +43,22 @@ __global__ void twiddle_kernel(Twiddle* out, int n) {
     Twiddle w;
     w.c = cf; w.s = sf; w.d = (float)(1.0 / m2 - 1.0); w.pad = 0.f;
     out[e] = w;
+}
+
+// outer twiddles of one FFT pass over blocks of length L with radix 16:
+// out[r * (L/16) + off] = W_L^{off r}
+__global__ void pass_twiddle_kernel(Twiddle* out, int L) {
+    int lr = L / 16;
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 16 * lr) return;
+    int r = idx / lr, off = idx - r * lr;
+    double s, c;
+    sincospi(-2.0 * (double)(off * r) / (double)L, &s, &c);
+    float cf = (float)c, sf = (float)s;
+    double m2 = (double)cf * (double)cf + (double)sf * (double)sf;
+    Twiddle w;
+    w.c = cf; w.s = sf; w.d = (float)(1.0 / m2 - 1.0); w.pad = 0.f;
+    out[idx] = w;
 }
 
 int fail(optifax_context* h, int code, const std::string& msg) {
@@ -64,6 +83,22 @@ const Twiddle* get_twiddles(optifax_context* h, int n, cudaStream_t st, int* rc)
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { cudaFree(d); *rc = cuda_fail(h, e, "twiddle_kernel sync"); return nullptr; }
     h->tw[n] = d;
+    return d;
+}
+
+const Twiddle* get_pass_twiddles(optifax_context* h, int M, cudaStream_t st, int* rc) {
+    auto it = h->passtw.find(M);
+    if (it != h->passtw.end()) return it->second;
+    int n1 = M, n2 = 16 * (M / 256);
+    Twiddle* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(Twiddle) * (size_t)(n1 + n2));
+    if (e != cudaSuccess) { *rc = cuda_fail(h, e, "cudaMalloc(pass twiddles)"); return nullptr; }
+    pass_twiddle_kernel<<<(n1 + 255) / 256, 256, 0, st>>>(d, M);
+    pass_twiddle_kernel<<<(n2 + 255) / 256, 256, 0, st>>>(d + n1, M / 16);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { cudaFree(d); *rc = cuda_fail(h, e, "pass_twiddle_kernel"); return nullptr; }
+    h->passtw[M] = d;
     return d;
 }
 
@@ -130,11 +165,26 @@ int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, 
     if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
                          "no kernel for cta_points=" + std::to_string(M) + " cluster=" + std::to_string(C));
     int rc = OPTIFAX_OK;
-    const Twiddle* twM = get_twiddles(h, M, st, &rc);
-    if (!twM) return rc;
-    const Twiddle* twN = (C > 1) ? get_twiddles(h, M * C, st, &rc) : twM;
+    const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
+    if (!twp) return rc;
+    const Twiddle* twN = get_twiddles(h, M * C, st, &rc);
     if (!twN) return rc;
-    size_t nb = descs.size() * sizeof(PulseDev);
+    FftTables tabs;
+    tabs.tw1 = twp;
+    tabs.tw2 = twp + M;
+    tabs.twN = twN;
+    std::vector<PulseDev> dv(descs);
+    if (C > 1) {
+        size_t need = dv.size() * 2 * (size_t)M * C;
+        if (need > h->xch_cap) {
+            if (h->d_xch) { cudaStreamSynchronize(st); cudaFree(h->d_xch); h->d_xch = nullptr; h->xch_cap = 0; }
+            cudaError_t e = cudaMalloc(&h->d_xch, need * sizeof(float2));
+            if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(exchange scratch)");
+            h->xch_cap = need;
+        }
+        for (size_t i = 0; i < dv.size(); ++i) dv[i].xch = h->d_xch + i * 2 * (size_t)M * C;
+    }
+    size_t nb = dv.size() * sizeof(PulseDev);
     if (nb > h->desc_cap) {
         if (h->d_desc) { cudaStreamSynchronize(st); cudaFree(h->d_desc); h->d_desc = nullptr; }
         size_t cap = nb < 4096 ? 4096 : nb * 2;
@@ -142,7 +192,7 @@ int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, 
         if (e != cudaSuccess) { h->desc_cap = 0; return cuda_fail(h, e, "cudaMalloc(descriptors)"); }
         h->desc_cap = cap;
     }
-    cudaError_t e = cudaMemcpyAsync(h->d_desc, descs.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaError_t e = cudaMemcpyAsync(h->d_desc, dv.data(), nb, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(descriptors)");
     if (shared) {
         e = cudaMemsetAsync(h->d_grid_flags, 0, 4 * sizeof(int), st);
@@ -181,7 +231,7 @@ int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, 
     lc.attrs = attrs;
     lc.numAttrs = na;
     const PulseDev* dd = h->d_desc;
-    e = cudaLaunchKernelEx(&lc, ke->fn, dd, twM, twN, cfg);
+    e = cudaLaunchKernelEx(&lc, ke->fn, dd, tabs, cfg);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaLaunchKernelEx(pass_kernel)");
     return OPTIFAX_OK;
 }
@@ -261,8 +311,10 @@ int optifax_destroy(optifax_handle h) {
     cudaSetDevice(h->device);
     cudaDeviceSynchronize();
     for (auto& kv : h->tw) cudaFree(kv.second);
+    for (auto& kv : h->passtw) cudaFree(kv.second);
     if (h->d_desc) cudaFree(h->d_desc);
     if (h->d_grid_flags) cudaFree(h->d_grid_flags);
+    if (h->d_xch) cudaFree(h->d_xch);
     delete h;
     return OPTIFAX_OK;
 }

@@ -7,7 +7,7 @@
 
 namespace ofx {
 
-typedef void (*KernelFn)(const PulseDev*, const Twiddle*, const Twiddle*, KernelCfg);
+typedef void (*KernelFn)(const PulseDev*, FftTables, KernelCfg);
 
 struct KernelEntry { KernelFn fn; size_t smem; int M, C, method; };
 

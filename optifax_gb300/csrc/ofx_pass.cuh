@@ -61,6 +61,14 @@ struct PulseDev {
     optifax_trip_record* trips;
     int n_trips, n_tally, steady_trips, steady_tally;
     float steady_tol;
+    // cluster (C > 1) exchange scratch in global memory: 2 N complex
+    float2* xch;
+};
+
+struct FftTables {
+    const Twiddle* tw1;      // pass-1 outer twiddles [16][M/16]: W_M^{off r}
+    const Twiddle* tw2;      // pass-2 outer twiddles [16][M/256]: W_{M/16}^{off r}
+    const Twiddle* twN;      // W_N^e, e in [0, N/2): cluster exchange
 };
 
 struct KernelCfg {
@@ -108,8 +116,31 @@ __device__ __forceinline__ float abc_factor(int i, int n, int mode) {
     return th * th;
 }
 
+// Error class of one point: pct = scale |d| / (|e| + 1) against the percent
+// thresholds (OPO_CUDA_BATCH_XTAL.cu:325-349; points with |e| == 0 skipped).
+// Compared in squares so only |e| needs a square root.
+__device__ __forceinline__ int classify(float scale, float2 d, float2 e, float maxE, float minE) {
+    float e2 = e.x * e.x + e.y * e.y;
+    int bits = 0;
+    if (e2 > 0.f) {
+        float den = sqrtf(e2) + 1.f;
+        float lhs = scale * scale * (d.x * d.x + d.y * d.y);
+        float hi = maxE * den, lo = minE * den;
+        if (maxE <= 0.f || lhs >= hi * hi) bits = 1;
+        else if (minE <= 0.f || lhs >= lo * lo) bits = 2;
+    }
+    if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
+    return bits;
+}
+
+// 16-byte stores of consecutive complex pairs to global memory (L2 only)
+__device__ __forceinline__ void store_pair(float2* base, int j, float2 v, float2& prev) {
+    if (j & 1) __stcg(reinterpret_cast<float4*>(base) + (j >> 1), make_float4(prev.x, prev.y, v.x, v.y));
+    else prev = v;
+}
+
 __device__ __forceinline__ float2 zphase(uint64_t tau_z4, float pos) {
-    uint64_t p4 = (uint64_t)(4.0f * pos);
+    uint64_t p4 = (uint64_t)(uint32_t)(4.0f * pos);
     return turn_to_unit((uint64_t)0 - tau_z4 * p4);
 }
 
@@ -125,7 +156,8 @@ struct Smem {
     static constexpr size_t off_tau = off_buf + sizeof(float2) * PADM * NBUF;
     static constexpr size_t off_l2a = off_tau + sizeof(uint64_t) * M;
     static constexpr size_t off_papp = off_l2a + sizeof(float) * M;
-    static constexpr size_t off_edge = off_papp + sizeof(uint64_t) * M;
+    static constexpr size_t off_abc = off_papp + sizeof(uint32_t) * M;
+    static constexpr size_t off_edge = off_abc + sizeof(float) * M;
     static constexpr size_t off_red = off_edge + sizeof(float2) * 4 * T;
     static constexpr size_t off_dred = off_red + 256;               // FP64 reduction slots
     static constexpr size_t bytes = off_dred + sizeof(double) * (8 * 4 + 2 * 16 * 4 + 4);
@@ -172,12 +204,16 @@ __device__ __forceinline__ float2 twn_inv(float2 v, const Twiddle* __restrict__ 
     return tw_inv(v, tw[e]);
 }
 
-// Four-step split of the N = C M transform: forward step 1 (C-point DFTs
-// over CTAs, twiddle W_N^{n2 k1}) from every CTA's E buffer into the X
-// buffers; each CTA handles the n2 slice [c M/C, (c+1) M/C).
+// Four-step split of the N = C M transform through global memory (L2):
+// forward step 1 (C-point DFTs over CTAs, twiddle W_N^{n2 k1}).  L2 moves the
+// field between the CTAs of a cluster far faster than distributed shared
+// memory: each CTA reads C slices of the other blocks, computes the C-point
+// DFTs of its n2 slice and writes the results to their owners' blocks.
+// Ordering comes from the cluster barriers around the calls (release/acquire
+// at cluster scope covers global memory); loads and stores bypass L1.
 template <int M, int C>
-__device__ __forceinline__ void exchange_forward(const float2* bufE, float2* bufX,
-                                                 const Twiddle* __restrict__ twN, int t, int c) {
+__device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx, float2* __restrict__ yy,
+                                                   const Twiddle* __restrict__ twN, int t, int c) {
     if constexpr (C > 1) {
         constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
 #pragma unroll
@@ -185,24 +221,20 @@ __device__ __forceinline__ void exchange_forward(const float2* bufE, float2* buf
             int n2 = c * (M / C) + t + T * u;
             float2 v[C];
 #pragma unroll
-            for (int n1 = 0; n1 < C; ++n1) v[n1] = remote<C>(bufE, n1)[phys(n2)];
+            for (int n1 = 0; n1 < C; ++n1) v[n1] = __ldcg(xx + n1 * M + n2);
             dif_stages<N, C, C>(v, 0, twN);
 #pragma unroll
             for (int r = 0; r < C; ++r) {
                 int k1 = bitrev(r, LOGC);
-                remote<C>(bufX, k1)[phys(n2)] = twn_fwd(v[r], twN, n2 * k1, N / 2);
+                __stcg(yy + k1 * M + n2, twn_fwd(v[r], twN, n2 * k1, N / 2));
             }
         }
     }
 }
 
-// Inverse of exchange_forward: from every CTA's X buffer (local inverse
-// transforms, natural n2 order), scaled by 1/N and either added to the E
-// buffers (which still hold the field an increment applies to) or stored.
 template <int M, int C>
-__device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* bufE,
-                                                 const Twiddle* __restrict__ twN, int t, int c, float invN,
-                                                 bool accumulate) {
+__device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy, float2* __restrict__ xx,
+                                                   const Twiddle* __restrict__ twN, int t, int c, float invN) {
     if constexpr (C > 1) {
         constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
 #pragma unroll
@@ -212,14 +244,11 @@ __device__ __forceinline__ void exchange_inverse(const float2* bufX, float2* buf
 #pragma unroll
             for (int r = 0; r < C; ++r) {
                 int k1 = bitrev(r, LOGC);
-                v[r] = twn_inv(remote<C>(bufX, k1)[phys(n2)], twN, n2 * k1, N / 2);
+                v[r] = twn_inv(__ldcg(yy + k1 * M + n2), twN, n2 * k1, N / 2);
             }
             dit_stages<N, C, C>(v, 0, twN);
 #pragma unroll
-            for (int n1 = 0; n1 < C; ++n1) {
-                float2* dst = remote<C>(bufE, n1) + phys(n2);
-                *dst = accumulate ? cadd(*dst, cscale(v[n1], invN)) : cscale(v[n1], invN);
-            }
+            for (int n1 = 0; n1 < C; ++n1) __stcg(xx + n1 * M + n2, cscale(v[n1], invN));
         }
     }
 }
@@ -308,8 +337,7 @@ __device__ __forceinline__ void reduce_tallies(const float (&part)[4], double (&
 // pump by the host.  Per-trip energy tallies sum tally_w |X|^2 in FP64.
 template <int M, int C, int METHOD>
 __global__ void __launch_bounds__(M / 16, 1)
-pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM,
-            const Twiddle* __restrict__ twN, KernelCfg cfg) {
+pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) {
     constexpr int T = M / 16;
     constexpr int N = M * C;
     constexpr int LOG2M = FftShape<M>::LOG2M;
@@ -320,7 +348,11 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
     float2* bufK = bufX + SM::PADM;   // RK23 only: FSAL K1 (own points)
     uint64_t* tau_s = reinterpret_cast<uint64_t*>(smem + SM::off_tau);
     float* l2a_s = reinterpret_cast<float*>(smem + SM::off_l2a);
-    uint64_t* papp_s = reinterpret_cast<uint64_t*>(smem + SM::off_papp);
+    uint32_t* papp_s = reinterpret_cast<uint32_t*>(smem + SM::off_papp);
+    float* abc_s = reinterpret_cast<float*>(smem + SM::off_abc);
+    const Twiddle* __restrict__ tw1 = tabs.tw1;
+    const Twiddle* __restrict__ tw2 = tabs.tw2;
+    const Twiddle* __restrict__ twN = tabs.twN;
     float2* edge = reinterpret_cast<float2*>(smem + SM::off_edge);
     int* red = reinterpret_cast<int*>(smem + SM::off_red);
     double* dred = reinterpret_cast<double*>(smem + SM::off_dred);
@@ -339,6 +371,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
         uint64_t jt = (uint64_t)time_index(i, N, cfg.time_mode);
         cph[j] = turn_to_unit(P.tau_theta * jt);
         a[j] = P.E_in[i];
+        abc_s[j * T + t] = abc_factor(i, N, cfg.abc_mode);
     }
 #pragma unroll 1
     for (int j = 0; j < 16; ++j) {
@@ -420,22 +453,17 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
 #pragma unroll
                     for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], k1[j]), cph[j], z);
                     exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+                    float2 prev;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         float2 k2 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
                         float2 e = cadd(a[j], cadd(cscale(k2, 0.5f), cscale(k1[j], 0.5f)));
-                        float2 d = cscale(csub(k2, k1[j]), 0.5f);          // = E - A1
-                        float ae = cabsf2(e);
-                        if (ae > 0.f) {
-                            float pct = 100.f * (cabsf2(d) / (ae + 1.f));
-                            if (pct >= maxE) bits |= 1;
-                            else if (pct >= minE) bits |= 2;
-                        }
-                        if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
-                        int i = c * M + 16 * t + j;
-                        float2 ea = cscale(e, abc_factor(i, N, cfg.abc_mode));
+                        float2 d = csub(k2, k1[j]);                        // = 2 (E - A1)
+                        bits |= classify(50.f, d, e, maxE, minE);
+                        float2 ea = cscale(e, abc_s[j * T + t]);
                         bufE[phys(16 * t + j)] = ea;
                         if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
+                        else store_pair(P.xch + c * M + 16 * t, j, ea, prev);
                     }
                 } else {
                     // ---- RK23: K2 at k + s/2, K3 at k + 3s/4, K4 at k + s (FSAL) ----
@@ -465,21 +493,16 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
 #pragma unroll
                     for (int j = 0; j < 16; ++j) nl[j] = nl_eval(ev[j], cph[j], z);
                     exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
+                    float2 prev;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         float2 k4 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
                         float2 d = csub(pp[j], cscale(k4, 1.f / 8.f));  // = E - A1
-                        float ae = cabsf2(ev[j]);
-                        if (ae > 0.f) {
-                            float pct = 200.f * (cabsf2(d) / (ae + 1.f));
-                            if (pct >= maxE) bits |= 1;
-                            else if (pct >= minE) bits |= 2;
-                        }
-                        if (!(isfinite(ev[j].x) && isfinite(ev[j].y))) bits |= 4;
-                        int i = c * M + 16 * t + j;
-                        float2 ea = cscale(ev[j], abc_factor(i, N, cfg.abc_mode));
+                        bits |= classify(200.f, d, ev[j], maxE, minE);
+                        float2 ea = cscale(ev[j], abc_s[j * T + t]);
                         bufE[phys(16 * t + j)] = ea;
                         if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
+                        else store_pair(P.xch + c * M + 16 * t, j, ea, prev);
                         bufK[phys(16 * t + j)] = k4;   // FSAL candidate (own points)
                     }
                 }
@@ -544,14 +567,15 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                     // |D - 1| instead of |E|.  At the end of an OPO pass the full
                     // spectrum goes through the cavity instead: A_new = IFFT(D FFT(E) fb + pump) / N.
                     float2* fbuf = (C > 1) ? bufX : bufE;
+                    float2* ybuf = (C > 1) ? P.xch + N + c * M : nullptr;
                     if constexpr (C > 1) {
-                        exchange_forward<M, C>(bufE, bufX, twN, t, c);
+                        exchange_forward_g<M, C>(P.xch, P.xch + N, twN, t, c);
                         cg::this_cluster().sync();
                     } else {
                         __syncthreads();
                     }
                     float2 v[16];
-                    fft_forward_to_regs<M>(fbuf, twM, t, v);
+                    fft_forward_to_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
                     float part[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -559,21 +583,38 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                         // phase increment beta*s from the exact fixed-point target minus the
                         // phase applied so far (error feedback: FP32 rounding of the
                         // increment is carried into the next step instead of accumulating)
-                        uint64_t target = tau_s[j * T + t] * (uint64_t)qn;
-                        uint64_t papp = papp_s[j * T + t];
-                        long long dfix = (long long)(target - papp);
-                        float df = (float)dfix;                       // units of 2^-64 turn
-                        if (df >= 0x1p63f) df = 0x1.fffffep62f;
-                        papp_s[j * T + t] = papp + (uint64_t)(long long)df;
-                        float s2, c2;
-                        sincospif(df * 0x1p-64f, &s2, &c2);           // sin, cos of (beta s)/2
-                        float2 dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);   // exp(-i beta s) - 1
                         float l2 = l2a_s[j * T + t];
-                        if (l2 != 0.f) {
-                            float x = (float)s_used * l2;
-                            float as = exp2f(x);
-                            float am1 = expm1f(x * 0.69314718055994531f);
-                            dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
+                        float2 dm1;
+                        if (l2 == -INFINITY) {
+                            dm1 = make_float2(-1.f, 0.f);                  // alpha = 0: D = 0
+                        } else {
+                            uint64_t target = tau_s[j * T + t] * (uint64_t)qn;
+                            uint32_t ph = papp_s[j * T + t];         // applied phase, 2^-32 turn units
+                            long long dfix = (long long)(target - ((uint64_t)ph << 32));
+                            int d32 = (int)(dfix >> 32);
+                            float df = (float)d32;
+                            if (df >= 2147483648.f) df = 2147483520.f;
+                            papp_s[j * T + t] = ph + (uint32_t)__float2int_rn(df);
+                            float th = df * 1.4629180792671596e-09f;  // radians (2 pi 2^-32 per unit)
+                            if (fabsf(th) < 0.25f) {
+                                // exp(-i th) - 1 by its Taylor series (no cancellation)
+                                float t2 = th * th;
+                                float cm1 = t2 * fmaf(t2, fmaf(t2, fmaf(t2, 2.48015873e-05f, -1.38888889e-03f),
+                                                               4.16666667e-02f), -0.5f);
+                                float sn = th * fmaf(t2, fmaf(t2, fmaf(t2, -1.98412698e-04f, 8.33333333e-03f),
+                                                              -1.66666667e-01f), 1.f);
+                                dm1 = make_float2(cm1, -sn);
+                            } else {
+                                float s2, c2;
+                                sincospif(df * 0x1p-32f, &s2, &c2);   // sin, cos of (beta s)/2
+                                dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);   // exp(-i beta s) - 1
+                            }
+                            if (l2 != 0.f) {
+                                float x = (float)s_used * l2;
+                                float as = exp2f(x);
+                                float am1 = expm1f(x * 0.69314718055994531f);
+                                dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
+                            }
                         }
                         float2 eh = v[j];
                         int kk = c + C * bitrev(16 * t + j, LOG2M);
@@ -589,13 +630,19 @@ pass_kernel(const PulseDev* __restrict__ pulses, const Twiddle* __restrict__ twM
                             v[j] = cmul(eh, dm1);
                         }
                     }
-                    fft_inverse_from_regs<M>(fbuf, twM, t, v);
+                    fft_inverse_from_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     if constexpr (C > 1) {
                         cg::this_cluster().sync();
-                        exchange_inverse<M, C>(bufX, bufE, twN, t, c, invN, !cav);
+                        exchange_inverse_g<M, C>(P.xch + N, P.xch, twN, t, c, invN);
                         cg::this_cluster().sync();
+                        const float4* src = reinterpret_cast<const float4*>(P.xch + c * M + 16 * t);
 #pragma unroll
-                        for (int j = 0; j < 16; ++j) a[j] = bufE[phys(16 * t + j)];
+                        for (int j = 0; j < 8; ++j) {
+                            float4 w = __ldcg(src + j);
+                            float2 d0 = make_float2(w.x, w.y), d1 = make_float2(w.z, w.w);
+                            a[2 * j] = cav ? d0 : cadd(bufE[phys(16 * t + 2 * j)], d0);
+                            a[2 * j + 1] = cav ? d1 : cadd(bufE[phys(16 * t + 2 * j + 1)], d1);
+                        }
                     } else {
                         if (cav) {
 #pragma unroll
