@@ -1,0 +1,120 @@
+"""Known-answer tests of the FP64 oracle (CPU).
+
+The reference ships no golden vectors for this path, so the restatement is
+checked against answers that follow from the equations themselves.
+"""
+import numpy as np
+import pytest
+
+from tests._cases import make_case, rel_l2
+
+
+def _run(orc, si, E, **kw):
+    args = dict(w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps, dt=si.dt,
+                max_err=si.max_err, min_err=si.min_err, sel=si.sel)
+    args.update(kw)
+    return orc.run(E, si.alpha, si.G, si.beta, **args)
+
+
+def test_fft_matches_numpy(oracle):
+    rng = np.random.default_rng(0)
+    for n in (8, 256, 4096):
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        assert np.max(np.abs(oracle.fft(x) - np.fft.fft(x))) < 1e-12 * n
+        assert np.max(np.abs(oracle.fft(x, inverse=True) - np.fft.ifft(x) * n)) < 1e-12 * n
+
+
+def test_pure_dispersion_is_exact(oracle):
+    """chi2 = 0 and no absorber: the pass is exp(-i beta q) alpha^q per mode, q = sum of stepmods."""
+    win, si, E = make_case(N=512, length=0.05e-3)
+    G0 = np.zeros_like(si.G)
+    r = oracle.run(E, si.alpha, G0, si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps,
+                   dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=si.sel,
+                   abc_mode=oracle.ABC_NONE, time_mode=oracle.TIME_UNSHIFTED, chunk_mode=oracle.CHUNKS_TRUNC)
+    q = r.stats[0]["z_steps"]
+    beta = si.beta.astype(np.float64)
+    expect = np.fft.ifft(np.fft.fft(E[0]) * np.exp(-1j * beta * q) * si.alpha.astype(np.float64) ** q)
+    assert rel_l2(r.A[0], expect) < 1e-12
+    assert r.stats[0]["rejected"] == 0
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_convergence_order(oracle, method):
+    """Fixed step (no rejection, no growth): the pass converges as h -> 0.  The
+    nonlinear and linear sub-steps are applied one after the other (Lie
+    splitting) and the poling sign is frozen at the start of each step, so the
+    global order is one whatever the stage scheme."""
+    errs = []
+    ref = None
+    base = dict(N=512, length=0.05e-3, power=2.0)
+    for f in (8, 1, 2, 4):
+        win, si, E = make_case(**base)
+        h = si.h / f
+        S = si.n_steps * f
+        G = np.repeat(si.G, f)
+        beta = (si.beta.astype(np.float64) / f)
+        alpha = si.alpha.astype(np.float64) ** (1.0 / f)
+        r = oracle.run(E, alpha, G, beta, w0=si.w0, bdiffw0=si.bdiffw0, h=h, n_steps=S, dt=si.dt,
+                       max_err=1e30, min_err=0.0, sel=float(S), method=method,
+                       abc_mode=oracle.ABC_NONE, time_mode=oracle.TIME_UNSHIFTED, chunk_mode=oracle.CHUNKS_TRUNC)
+        if ref is None:
+            ref = r.A[0]
+        else:
+            errs.append(rel_l2(r.A[0], ref))
+    assert errs[0] > errs[1] > errs[2], errs
+    rate = np.log2(errs[0] / errs[2]) / 2.0
+    assert rate > 0.8, (errs, rate)
+
+
+def test_energy_balance_converged(oracle):
+    """The model's energy balance (G33 is evaluated at w0, so sum |E|^2 is not an
+    exact invariant of the equations) does not depend on the step schedule once
+    the steps are small: default and tight tolerances agree."""
+    out = []
+    for eb in [(2.5e-3, 5e-2), (1e-6, 2e-5)]:
+        win, si, E = make_case(N=1024, length=0.1e-3, power=1.0, error_bounds=eb)
+        r = oracle.run(E, si.alpha, si.G, si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps,
+                       dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=si.sel,
+                       abc_mode=oracle.ABC_NONE, time_mode=oracle.TIME_UNSHIFTED, chunk_mode=oracle.CHUNKS_TRUNC)
+        e_in = np.sum(np.abs(E[0]) ** 2)
+        out.append((np.sum(np.abs(r.A[0]) ** 2) - e_in) / e_in)
+    assert abs(out[0] - out[1]) < 0.05 * abs(out[1])
+
+
+def test_replay_reproduces_schedule(oracle):
+    """Replaying the recorded decisions reproduces the run bit for bit."""
+    win, si, E = make_case(N=512, length=0.1e-3, power=2.0)
+    r1 = _run(oracle, si, E[0], trace_cap=100000)
+    r2 = _run(oracle, si, E[0], trace_cap=100000, forced=r1.trace[0][:, 2] & 3)
+    assert np.array_equal(r1.A[0], r2.A[0])
+    assert np.array_equal(r1.trace[0], r2.trace[0])
+
+
+def test_reject_moves_k_back_by_one(oracle):
+    """MEX semantics (OPO_CUDA_BATCH_XTAL.cu:460-466): after a rejection the next
+    attempt starts at k-1 with stepmod-1."""
+    win, si, E = make_case(N=512, length=0.3e-3, power=3.0, error_bounds=(1e-6, 2e-5))
+    r = _run(oracle, si, E[0], trace_cap=100000)
+    tr = r.trace[0]
+    rej = np.where((tr[:, 2] & 8) == 0)[0]
+    assert len(rej) > 0
+    for i in rej[:50]:
+        if i + 1 < len(tr):
+            assert tr[i + 1, 0] == tr[i, 0] - 1 and tr[i + 1, 1] == tr[i, 1] - 1
+
+
+def test_nee_semantics_run(oracle):
+    """NEE_CPU.m schedule: rejection keeps k; chunks of sel; Ap written per chunk."""
+    win, si, E = make_case(N=512, length=0.1e-3, power=2.0)
+    r = oracle.run(E[0], si.alpha, si.G, si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                   n_steps=si.n_steps, dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=si.sel,
+                   method=oracle.HEUN_NEE, trace_cap=100000)
+    tr = r.trace[0]
+    rej = np.where((tr[:, 2] & 8) == 0)[0]
+    for i in rej:
+        if i + 1 < len(tr):
+            assert tr[i + 1, 0] == tr[i, 0]
+    assert r.stats[0]["status"] == 0
+    mex = _run(oracle, si, E[0])
+    # same physics, different conventions: close but not identical
+    assert 0 < rel_l2(r.A[0], mex.A[0]) < 0.5
