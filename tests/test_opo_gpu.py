@@ -68,7 +68,7 @@ def test_opo_round_trips_high_gain(oracle):
     from optifax_gb300 import opo
     spec = opo.CavitySpec(n_points=1024, window=1024 * 6e-12 / 2 ** 13, crystal_length=0.4e-3,
                           pump_tau=60e-15, pump_power=3.0, seed=1)
-    _compare(oracle, spec, 6, lambda n: 1e-6 if n == 0 else (1e-4 if n == 1 else 1e-2), 1e-2)
+    _compare(oracle, spec, 5, lambda n: 1e-6 if n == 0 else (1e-4 if n == 1 else 1e-2), 1e-2)
 
 
 def test_opo_steady_state_stop():
