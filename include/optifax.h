@@ -184,6 +184,28 @@ int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_p
 int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cavities,
                     int32_t variant, int32_t cta_points, optifax_pulse_stats* stats, void* stream);
 
+/*
+ * One crystal pass (Heun schedule) that allocates no device memory, for callers
+ * that cannot allocate GPU memory while they run -- a solver inside a MATLAB MEX
+ * function whose device memory belongs to MATLAB's gpuArray manager, an
+ * application that hands all device memory to its own caching allocator, or a
+ * latency-critical loop that cannot let cudaMalloc/cudaFree synchronise the
+ * device.  This entry point has no counterpart in the reference.
+ *
+ * The caller passes the pulse's inputs and outputs (device pointers, as for
+ * optifax_propagate; stats optional) and no handle.  The descriptor, twiddle
+ * tables and cluster exchange buffer live in one static device array of about
+ * 0.45 MB that each GPU loading the library reserves until the process exits.
+ * n_points must be 8192 or 16384 (clusters of 2 or 4 CTAs of 4096 points);
+ * other sizes, including anything above 16384, return OPTIFAX_ERR_UNSUPPORTED.
+ * Variants BATCH_XTAL, BATCH_OP, NO_BC and HARD_BC are accepted.  The first call
+ * on a device builds the twiddle tables in the array (set-up) and should come
+ * before any stream capture.  Every call reuses the same array: calls that
+ * overlap on the GPU race and must be serialised by the caller.
+ */
+int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t variant,
+                              optifax_pulse_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

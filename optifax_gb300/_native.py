@@ -15,7 +15,7 @@ VARIANT_BATCH_XTAL, VARIANT_BATCH_OP, VARIANT_NO_BC, VARIANT_HARD_BC, VARIANT_OD
 PULSE_NAN, PULSE_ATTEMPT_LIMIT = 0x1, 0x2
 
 EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifax_last_error",
-           "optifax_opo_mex_batch", "optifax_propagate"]
+           "optifax_opo_mex_batch", "optifax_propagate", "optifax_opo_run", "optifax_propagate_noalloc"]
 
 _lib = None
 
@@ -73,6 +73,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_opo_mex_batch.restype = ctypes.c_int
     lib.optifax_propagate.argtypes = [vp, ctypes.POINTER(OptifaxPulse), i32, i32, i32, i32, vp, vp]
     lib.optifax_propagate.restype = ctypes.c_int
+    lib.optifax_propagate_noalloc.argtypes = [ctypes.POINTER(OptifaxPulse), i32, vp, vp]
+    lib.optifax_propagate_noalloc.restype = ctypes.c_int
     _lib = lib
     return lib
 
