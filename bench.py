@@ -136,6 +136,35 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def pass_case(n_points: int, length: float, cta_points: int, reps: int = 2):
+    """Profiling case: one crystal pass of a sech^2 pump + noise (dt = 6 ps / 2^13,
+    30 um PPLN, 2 W) run `reps` times; prints per-attempt device time."""
+    import numpy as np
+    import torch
+    from optifax_gb300 import physics as ph, solver as sv, _native as nat
+    win = ph.SimWindow(1040e-9, n_points, n_points * 6e-12 / 2 ** 13)
+    si = ph.solver_inputs(ph.Crystal(length, 30e-6), win)
+    tau = min(200e-15, win.temporal_range / 12)
+    e = np.fft.fftshift(ph.sech_pump(win, 1040e-9, tau, 2.0) +
+                        ph.photon_noise(win, 0, mask=ph.window_transmission(win)))
+    e = np.fft.ifft(np.fft.fft(e) * np.sqrt(1.0 / si.n_index))
+    dev = torch.device("cuda:0")
+    spec = sv.PulseSpec(E=torch.from_numpy(e.astype(np.complex64)).to(dev),
+                        alpha=torch.from_numpy(si.alpha).to(dev), beta=torch.from_numpy(si.beta).to(dev),
+                        G=torch.from_numpy(si.G).to(dev), w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, dt=si.dt,
+                        max_err=si.max_err, min_err=si.min_err, sel=si.sel, n_steps=si.n_steps)
+    for _ in range(reps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        _, stats = sv.propagate([spec], method=nat.HEUN, variant=nat.VARIANT_BATCH_XTAL, cta_points=cta_points)
+        ev1.record()
+        torch.cuda.synchronize()
+        st = sv.decode_stats(stats)[0]
+        ms = ev0.elapsed_time(ev1)
+        print(json.dumps({"case": "pass", "n_points": n_points, "length_m": length, "cta_points": cta_points,
+                          "attempts": st["attempts"], "ms": ms, "us_per_attempt": 1000 * ms / st["attempts"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -144,7 +173,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cta-points", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pass-case", default=None,
+                    help="profiling case 'N,length_m': one crystal pass, run twice, no JSON bench line")
     args = ap.parse_args()
+    if args.pass_case:
+        n, length = args.pass_case.split(",")
+        return pass_case(int(n), float(length), args.cta_points)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -133,6 +133,36 @@ __device__ __forceinline__ int classify(float scale, float2 d, float2 e, float m
     return bits;
 }
 
+// D - 1 = alpha^s exp(-i th) - 1 for the phase increment d32 (units of 2^-32
+// turn; converted to FP32, *dapplied receives the integer actually used) and
+// log2 alpha l2 (-inf: alpha = 0).
+__device__ __forceinline__ float2 dispersion_dm1(int d32, float l2, int s, int* dapplied) {
+    if (l2 == -INFINITY) { *dapplied = d32; return make_float2(-1.f, 0.f); }
+    float df = (float)d32;
+    if (df >= 2147483648.f) df = 2147483520.f;
+    *dapplied = __float2int_rn(df);
+    float th = df * 1.4629180792671596e-09f;   // radians (2 pi 2^-32 per unit)
+    float2 dm1;
+    if (fabsf(th) < 0.25f) {
+        // exp(-i th) - 1 by its Taylor series (no cancellation)
+        float t2 = th * th;
+        float cm1 = t2 * fmaf(t2, fmaf(t2, fmaf(t2, 2.48015873e-05f, -1.38888889e-03f), 4.16666667e-02f), -0.5f);
+        float sn = th * fmaf(t2, fmaf(t2, fmaf(t2, -1.98412698e-04f, 8.33333333e-03f), -1.66666667e-01f), 1.f);
+        dm1 = make_float2(cm1, -sn);
+    } else {
+        float s2, c2;
+        sincospif(df * 0x1p-32f, &s2, &c2);   // sin, cos of th/2
+        dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);
+    }
+    if (l2 != 0.f) {
+        float x = (float)s * l2;
+        float as = exp2f(x);
+        float am1 = expm1f(x * 0.69314718055994531f);
+        dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
+    }
+    return dm1;
+}
+
 // 16-byte stores of consecutive complex pairs to global memory (L2 only)
 __device__ __forceinline__ void store_pair(float2* base, int j, float2 v, float2& prev) {
     if (j & 1) __stcg(reinterpret_cast<float4*>(base) + (j >> 1), make_float4(prev.x, prev.y, v.x, v.y));
@@ -157,7 +187,11 @@ struct Smem {
     static constexpr size_t off_l2a = off_tau + sizeof(uint64_t) * M;
     static constexpr size_t off_papp = off_l2a + sizeof(float) * M;
     static constexpr size_t off_abc = off_papp + sizeof(uint32_t) * M;
-    static constexpr size_t off_edge = off_abc + sizeof(float) * M;
+    // Heun: per-mode D - 1 and its fixed-point phase increment for the cached stepmod
+    static constexpr int NCACHE = (METHOD == OPTIFAX_HEUN) ? M : 0;
+    static constexpr size_t off_dmc = off_abc + sizeof(float) * M;
+    static constexpr size_t off_dfc = off_dmc + sizeof(float2) * NCACHE;
+    static constexpr size_t off_edge = off_dfc + sizeof(int) * NCACHE;
     static constexpr size_t off_red = off_edge + sizeof(float2) * 4 * T;
     static constexpr size_t off_dred = off_red + 256;               // FP64 reduction slots
     static constexpr size_t bytes = off_dred + sizeof(double) * (8 * 4 + 2 * 16 * 4 + 4);
@@ -216,17 +250,19 @@ __device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx
                                                    const Twiddle* __restrict__ twN, int t, int c) {
     if constexpr (C > 1) {
         constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
+        float2 v[PER][C];
+#pragma unroll
+        for (int u = 0; u < PER; ++u)          // every load in flight before any use
+#pragma unroll
+            for (int n1 = 0; n1 < C; ++n1) v[u][n1] = __ldcg(xx + n1 * M + c * (M / C) + t + T * u);
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
             int n2 = c * (M / C) + t + T * u;
-            float2 v[C];
-#pragma unroll
-            for (int n1 = 0; n1 < C; ++n1) v[n1] = __ldcg(xx + n1 * M + n2);
-            dif_stages<N, C, C>(v, 0, twN);
+            dif_stages<N, C, C>(v[u], 0, twN);
 #pragma unroll
             for (int r = 0; r < C; ++r) {
                 int k1 = bitrev(r, LOGC);
-                __stcg(yy + k1 * M + n2, twn_fwd(v[r], twN, n2 * k1, N / 2));
+                __stcg(yy + k1 * M + n2, twn_fwd(v[u][r], twN, n2 * k1, N / 2));
             }
         }
     }
@@ -237,18 +273,19 @@ __device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy
                                                    const Twiddle* __restrict__ twN, int t, int c, float invN) {
     if constexpr (C > 1) {
         constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
+        float2 v[PER][C];
+#pragma unroll
+        for (int u = 0; u < PER; ++u)          // every load in flight before any use
+#pragma unroll
+            for (int r = 0; r < C; ++r) v[u][r] = __ldcg(yy + bitrev(r, LOGC) * M + c * (M / C) + t + T * u);
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
             int n2 = c * (M / C) + t + T * u;
-            float2 v[C];
 #pragma unroll
-            for (int r = 0; r < C; ++r) {
-                int k1 = bitrev(r, LOGC);
-                v[r] = twn_inv(__ldcg(yy + k1 * M + n2), twN, n2 * k1, N / 2);
-            }
-            dit_stages<N, C, C>(v, 0, twN);
+            for (int r = 0; r < C; ++r) v[u][r] = twn_inv(v[u][r], twN, n2 * bitrev(r, LOGC), N / 2);
+            dit_stages<N, C, C>(v[u], 0, twN);
 #pragma unroll
-            for (int n1 = 0; n1 < C; ++n1) __stcg(xx + n1 * M + n2, cscale(v[n1], invN));
+            for (int n1 = 0; n1 < C; ++n1) __stcg(xx + n1 * M + n2, cscale(v[u][n1], invN));
         }
     }
 }
@@ -350,6 +387,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
     float* l2a_s = reinterpret_cast<float*>(smem + SM::off_l2a);
     uint32_t* papp_s = reinterpret_cast<uint32_t*>(smem + SM::off_papp);
     float* abc_s = reinterpret_cast<float*>(smem + SM::off_abc);
+    float2* dmc_s = reinterpret_cast<float2*>(smem + SM::off_dmc);
+    int* dfc_s = reinterpret_cast<int*>(smem + SM::off_dfc);
     const Twiddle* __restrict__ tw1 = tabs.tw1;
     const Twiddle* __restrict__ tw2 = tabs.tw2;
     const Twiddle* __restrict__ twN = tabs.twN;
@@ -360,7 +399,13 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
     const int t = threadIdx.x;
     const int c = (C > 1) ? (int)cg::this_cluster().block_rank() : 0;
     const int p = blockIdx.x / C;
-    const PulseDev& P = pulses[p];
+    // The descriptor is read all through the loop; a shared-memory copy keeps
+    // those reads off the global path (and out of reach of aliasing with the
+    // kernel's global stores).
+    __shared__ PulseDev sP;
+    if (t == 0) sP = pulses[p];
+    __syncthreads();
+    const PulseDev& P = sP;
 
     // ---- prologue -------------------------------------------------------
     for (int i = t; i < 64; i += T) red[i] = 0;
@@ -403,6 +448,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
 
     float k = 0.f, stepprev = 4.f, stepmod = 4.f;
     unsigned q = 0;                          // accumulated dispersion position (sum of stepmod)
+    int s_cached = -1;                       // stepmod of the cached per-mode D - 1 (Heun)
     int attempt = 0, n_acc = 0, n_rej = 0, status = 0, par = 0, trip = 0, trips_done = 0;
     int gatt = 0, tot_att = 0, tot_acc = 0, tot_rej = 0, steady_count = 0;
     double prev_tally = 0.0;
@@ -583,39 +629,37 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                         // phase increment beta*s from the exact fixed-point target minus the
                         // phase applied so far (error feedback: FP32 rounding of the
                         // increment is carried into the next step instead of accumulating)
-                        float l2 = l2a_s[j * T + t];
+                        // increment beta*s: exact fixed-point target minus the phase applied
+                        // so far (error feedback: nothing accumulates from FP32 rounding)
+                        const int idx = j * T + t;
+                        uint64_t target = tau_s[idx] * (uint64_t)qn;
+                        uint32_t ph = papp_s[idx];
+                        int d32 = (int)((long long)(target - ((uint64_t)ph << 32)) >> 32);
                         float2 dm1;
-                        if (l2 == -INFINITY) {
-                            dm1 = make_float2(-1.f, 0.f);                  // alpha = 0: D = 0
+                        int dused;
+                        if constexpr (METHOD == OPTIFAX_HEUN) {
+                            // D - 1 cached per mode for the current stepmod; the small
+                            // difference eps between the wanted and the cached increment
+                            // is applied to first order: D e^{-i eps} - 1 ~ (D - 1) - i eps D
+                            if (s_used != s_cached) {
+                                int dc;
+                                uint64_t inc = tau_s[idx] * (uint64_t)(unsigned)s_used;
+                                dmc_s[idx] = dispersion_dm1((int)((long long)inc >> 32), l2a_s[idx], s_used, &dc);
+                                dfc_s[idx] = dc;
+                            }
+                            float2 dc1 = dmc_s[idx];
+                            int eps = d32 - dfc_s[idx];
+                            dm1 = dc1;
+                            if (eps != 0) {
+                                float e = (float)eps * 1.4629180792671596e-09f;
+                                float2 D = make_float2(1.f + dc1.x, dc1.y);
+                                dm1 = make_float2(fmaf(e, D.y, dc1.x), fmaf(-e, D.x, dc1.y));
+                            }
+                            dused = d32;
                         } else {
-                            uint64_t target = tau_s[j * T + t] * (uint64_t)qn;
-                            uint32_t ph = papp_s[j * T + t];         // applied phase, 2^-32 turn units
-                            long long dfix = (long long)(target - ((uint64_t)ph << 32));
-                            int d32 = (int)(dfix >> 32);
-                            float df = (float)d32;
-                            if (df >= 2147483648.f) df = 2147483520.f;
-                            papp_s[j * T + t] = ph + (uint32_t)__float2int_rn(df);
-                            float th = df * 1.4629180792671596e-09f;  // radians (2 pi 2^-32 per unit)
-                            if (fabsf(th) < 0.25f) {
-                                // exp(-i th) - 1 by its Taylor series (no cancellation)
-                                float t2 = th * th;
-                                float cm1 = t2 * fmaf(t2, fmaf(t2, fmaf(t2, 2.48015873e-05f, -1.38888889e-03f),
-                                                               4.16666667e-02f), -0.5f);
-                                float sn = th * fmaf(t2, fmaf(t2, fmaf(t2, -1.98412698e-04f, 8.33333333e-03f),
-                                                              -1.66666667e-01f), 1.f);
-                                dm1 = make_float2(cm1, -sn);
-                            } else {
-                                float s2, c2;
-                                sincospif(df * 0x1p-32f, &s2, &c2);   // sin, cos of (beta s)/2
-                                dm1 = make_float2(-2.f * s2 * s2, -2.f * s2 * c2);   // exp(-i beta s) - 1
-                            }
-                            if (l2 != 0.f) {
-                                float x = (float)s_used * l2;
-                                float as = exp2f(x);
-                                float am1 = expm1f(x * 0.69314718055994531f);
-                                dm1 = make_float2(fmaf(dm1.x, as, am1), dm1.y * as);
-                            }
+                            dm1 = dispersion_dm1(d32, l2a_s[idx], s_used, &dused);
                         }
+                        papp_s[idx] = ph + (uint32_t)dused;
                         float2 eh = v[j];
                         int kk = c + C * bitrev(16 * t + j, LOG2M);
                         if (apc) apc[kk] = cadd(eh, cmul(eh, dm1));
@@ -630,6 +674,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                             v[j] = cmul(eh, dm1);
                         }
                     }
+                    s_cached = s_used;
                     fft_inverse_from_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     if constexpr (C > 1) {
                         cg::this_cluster().sync();
