@@ -180,6 +180,53 @@ def pass_case(n_points: int, length: float, cta_points: int, reps: int = 2):
                           "attempts": st["attempts"], "ms": ms, "us_per_attempt": 1000 * ms / st["attempts"]}))
 
 
+def run_sweep(args):
+    """Config 3: a batch of crystal passes with uneven grids (2^12..2^16), crystals
+    (0.5-10 mm, 28-32 um), pumps (0.5-3 W, 100-300 fs), seed 2, in one call.
+    A step is one whole batch; value = instances per second."""
+    import numpy as np
+    import torch
+    from optifax_gb300 import sweep, solver as sv
+    insts = sweep.config3_instances(n=args.sweep_size, seed=2)
+    t0 = time.perf_counter()
+    inputs = [sweep.build_inputs(i) for i in insts]
+    prep_s = time.perf_counter() - t0
+    tuned = sv.autotune(sorted({i.n_points for i in insts}))
+    specs = sweep.to_specs(inputs)
+    stream = torch.cuda.current_stream()
+    for _ in range(1):
+        sv.propagate(specs, stream=stream)
+    torch.cuda.synchronize()
+    times, atts = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            _, st = sv.propagate(specs, stream=stream)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            times.append(ev0.elapsed_time(ev1) / 1000.0)
+            atts.append(sv.decode_stats(st))
+    t = float(np.mean(times))
+    stats = atts[-1]
+    point_attempts = sum(s_["attempts"] * i.n_points for s_, i in zip(stats, insts))
+    peak, peak_kind = _peaks()
+    achieved = 16.0 * point_attempts / t / 1e9
+    line = {"metric": "batched crystal passes/s (uneven sweep)", "value": len(insts) / t, "unit": "passes/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": t * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"config 3 sweep: {len(insts)} instances, N 2^12..2^16, L 0.5-10 mm, "
+                                   "period 28-32 um, 0.5-3 W, 100-300 fs, seed 2", "autotuned_cta_points": tuned,
+                       "host_prep_s": prep_s, "point_attempts": point_attempts,
+                       "attempts": int(sum(s_["attempts"] for s_ in stats))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic": "16 B per grid point per step attempt"},
+            "gpu_launches": len({(i.n_points) for i in insts}),
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,6 +235,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cta-points", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="opo", choices=["opo", "sweep"],
+                    help="opo: config-2 OPO round trips (default line); sweep: config-3 batched passes")
+    ap.add_argument("--sweep-size", type=int, default=256)
     ap.add_argument("--pass-case", default=None,
                     help="profiling case 'N,length_m': one crystal pass, run twice, no JSON bench line")
     args = ap.parse_args()
@@ -198,6 +248,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "sweep":
+        return run_sweep(args)
 
     import numpy as np
     import torch

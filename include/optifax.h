@@ -100,6 +100,7 @@ typedef struct {
     float min_err;           /* percent */
     float sel;               /* steps per progress chunk */
     int32_t stepmods_limit;  /* stepmods recorded for k < limit (0: the variant's own rule) */
+    int32_t cta_points;      /* points per CTA for this pulse (0: the call's choice) */
 } optifax_pulse;
 
 /*

@@ -30,7 +30,7 @@ class OptifaxPulse(ctypes.Structure):
                 ("w0", ctypes.c_float), ("h", ctypes.c_float),
                 ("bdiffw0", ctypes.c_double), ("dt", ctypes.c_double),
                 ("max_err", ctypes.c_float), ("min_err", ctypes.c_float), ("sel", ctypes.c_float),
-                ("stepmods_limit", ctypes.c_int32)]
+                ("stepmods_limit", ctypes.c_int32), ("cta_points", ctypes.c_int32)]
 
 
 class OptifaxPulseStats(ctypes.Structure):

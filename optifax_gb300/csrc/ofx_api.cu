@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -27,6 +28,8 @@ struct optifax_context {
     size_t desc_cap = 0;
     float2* d_xch = nullptr;             // cluster exchange scratch
     size_t xch_cap = 0;                  // in complex values
+    std::vector<cudaStream_t> side;      // streams for concurrent launch groups
+    std::vector<cudaEvent_t> ev;         // fork/join events
     int* d_grid_flags = nullptr;
     std::string last_error;
 };
@@ -158,82 +161,155 @@ int choose_M(int N, int cta_points) {
     return N <= 4096 ? N : 4096;
 }
 
-// Build descriptors of one launch group and launch it.
-int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, int C, int method,
-                 const VariantCfg& vc, bool shared, cudaStream_t st) {
-    const KernelEntry* ke = find_kernel(M, C, method);
-    if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
-                         "no kernel for cta_points=" + std::to_string(M) + " cluster=" + std::to_string(C));
-    int rc = OPTIFAX_OK;
-    const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
-    if (!twp) return rc;
-    const Twiddle* twN = get_twiddles(h, M * C, st, &rc);
-    if (!twN) return rc;
-    FftTables tabs;
-    tabs.tw1 = twp;
-    tabs.tw2 = twp + M;
-    tabs.twN = twN;
-    std::vector<PulseDev> dv(descs);
-    if (C > 1) {
-        size_t need = dv.size() * 2 * (size_t)M * C;
-        if (need > h->xch_cap) {
-            if (h->d_xch) { cudaStreamSynchronize(st); cudaFree(h->d_xch); h->d_xch = nullptr; h->xch_cap = 0; }
-            cudaError_t e = cudaMalloc(&h->d_xch, need * sizeof(float2));
-            if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(exchange scratch)");
-            h->xch_cap = need;
-        }
-        for (size_t i = 0; i < dv.size(); ++i) dv[i].xch = h->d_xch + i * 2 * (size_t)M * C;
+struct Group {
+    int M, C;
+    std::vector<PulseDev> d;
+};
+
+double pulse_cost(const PulseDev& d) {
+    return (double)d.N * std::log2((double)d.N) * (double)d.S;
+}
+
+int ensure_sync_objects(optifax_context* h, size_t n_streams) {
+    while (h->side.size() < n_streams) {
+        cudaStream_t s_;
+        cudaError_t e = cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamCreate");
+        h->side.push_back(s_);
     }
-    size_t nb = dv.size() * sizeof(PulseDev);
+    while (h->ev.size() < n_streams + 1) {
+        cudaEvent_t e_;
+        cudaError_t e = cudaEventCreateWithFlags(&e_, cudaEventDisableTiming);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventCreate");
+        h->ev.push_back(e_);
+    }
+    return OPTIFAX_OK;
+}
+
+// Stage every group's descriptors (longest work first within a group), then
+// launch one grid per (cta_points, cluster) group.  Groups after the first run
+// on side streams forked from and joined back into `st`, so the block
+// scheduler interleaves them: CTAs of a long group fill SMs as short ones end.
+int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, const VariantCfg& vc,
+                  bool shared, cudaStream_t st) {
+    size_t n_desc = 0, need_xch = 0;
+    for (auto& g : groups) {
+        std::stable_sort(g.d.begin(), g.d.end(),
+                         [](const PulseDev& x, const PulseDev& y) { return pulse_cost(x) > pulse_cost(y); });
+        n_desc += g.d.size();
+        if (g.C > 1) need_xch += g.d.size() * 2 * (size_t)g.M * g.C;
+    }
+    if (need_xch > h->xch_cap) {
+        if (h->d_xch) { cudaDeviceSynchronize(); cudaFree(h->d_xch); h->d_xch = nullptr; h->xch_cap = 0; }
+        cudaError_t e = cudaMalloc(&h->d_xch, need_xch * sizeof(float2));
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(exchange scratch)");
+        h->xch_cap = need_xch;
+    }
+    std::vector<PulseDev> all;
+    all.reserve(n_desc);
+    size_t xoff = 0;
+    for (auto& g : groups)
+        for (auto& d : g.d) {
+            if (g.C > 1) { d.xch = h->d_xch + xoff; xoff += 2 * (size_t)g.M * g.C; }
+            all.push_back(d);
+        }
+    size_t nb = all.size() * sizeof(PulseDev);
     if (nb > h->desc_cap) {
-        if (h->d_desc) { cudaStreamSynchronize(st); cudaFree(h->d_desc); h->d_desc = nullptr; }
+        if (h->d_desc) { cudaDeviceSynchronize(); cudaFree(h->d_desc); h->d_desc = nullptr; }
         size_t cap = nb < 4096 ? 4096 : nb * 2;
         cudaError_t e = cudaMalloc(&h->d_desc, cap);
         if (e != cudaSuccess) { h->desc_cap = 0; return cuda_fail(h, e, "cudaMalloc(descriptors)"); }
         h->desc_cap = cap;
     }
-    cudaError_t e = cudaMemcpyAsync(h->d_desc, dv.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaError_t e = cudaMemcpyAsync(h->d_desc, all.data(), nb, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(descriptors)");
     if (shared) {
         e = cudaMemsetAsync(h->d_grid_flags, 0, 4 * sizeof(int), st);
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync(grid flags)");
     }
-    e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ke->smem);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(smem)");
-    if (C > 8) {
-        e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(cluster 16)");
+    int rc = ensure_sync_objects(h, groups.size());
+    if (rc) return rc;
+    // tables first: building one synchronises the stream, which must not
+    // happen between the launches
+    std::vector<FftTables> tabv(groups.size());
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        const Twiddle* twp = get_pass_twiddles(h, groups[gi].M, st, &rc);
+        if (!twp) return rc;
+        const Twiddle* twN = get_twiddles(h, groups[gi].M * groups[gi].C, st, &rc);
+        if (!twN) return rc;
+        tabv[gi].tw1 = twp;
+        tabv[gi].tw2 = twp + groups[gi].M;
+        tabv[gi].twN = twN;
     }
-    KernelCfg cfg;
-    cfg.time_mode = vc.time_mode;
-    cfg.abc_mode = vc.abc_mode;
-    cfg.guard = vc.guard;
-    cfg.shared_sched = shared ? 1 : 0;
-    cfg.max_attempts_mul = 64;
-    cfg.grid_flags = h->d_grid_flags;
-
-    cudaLaunchConfig_t lc;
-    memset(&lc, 0, sizeof(lc));
-    lc.gridDim = dim3((unsigned)(descs.size() * C), 1, 1);
-    lc.blockDim = dim3(M / 16, 1, 1);
-    lc.dynamicSmemBytes = ke->smem;
-    lc.stream = st;
-    cudaLaunchAttribute attrs[2];
-    int na = 0;
-    attrs[na].id = cudaLaunchAttributeClusterDimension;
-    attrs[na].val.clusterDim.x = C; attrs[na].val.clusterDim.y = 1; attrs[na].val.clusterDim.z = 1;
-    ++na;
-    if (shared) {
-        attrs[na].id = cudaLaunchAttributeCooperative;
-        attrs[na].val.cooperative = 1;
+    if (groups.size() > 1) {
+        e = cudaEventRecord(h->ev[0], st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
+    }
+    size_t off = 0;
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+        Group& g = groups[gi];
+        const int M = g.M, C = g.C;
+        const KernelEntry* ke = find_kernel(M, C, method);
+        if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
+                             "no kernel for cta_points=" + std::to_string(M) + " cluster=" + std::to_string(C));
+        const FftTables tabs = tabv[gi];
+        e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ke->smem);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(smem)");
+        if (C > 8) {
+            e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(cluster 16)");
+        }
+        KernelCfg cfg;
+        cfg.time_mode = vc.time_mode;
+        cfg.abc_mode = vc.abc_mode;
+        cfg.guard = vc.guard;
+        cfg.shared_sched = shared ? 1 : 0;
+        cfg.max_attempts_mul = 64;
+        cfg.grid_flags = h->d_grid_flags;
+        cudaStream_t ls = st;
+        if (gi > 0) {
+            ls = h->side[gi - 1];
+            e = cudaStreamWaitEvent(ls, h->ev[0], 0);
+            if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamWaitEvent(fork)");
+        }
+        cudaLaunchConfig_t lc;
+        memset(&lc, 0, sizeof(lc));
+        lc.gridDim = dim3((unsigned)(g.d.size() * C), 1, 1);
+        lc.blockDim = dim3(M / 16, 1, 1);
+        lc.dynamicSmemBytes = ke->smem;
+        lc.stream = ls;
+        cudaLaunchAttribute attrs[2];
+        int na = 0;
+        attrs[na].id = cudaLaunchAttributeClusterDimension;
+        attrs[na].val.clusterDim.x = C; attrs[na].val.clusterDim.y = 1; attrs[na].val.clusterDim.z = 1;
         ++na;
+        if (shared) {
+            attrs[na].id = cudaLaunchAttributeCooperative;
+            attrs[na].val.cooperative = 1;
+            ++na;
+        }
+        lc.attrs = attrs;
+        lc.numAttrs = na;
+        const PulseDev* dd = h->d_desc + off;
+        e = cudaLaunchKernelEx(&lc, ke->fn, dd, tabs, cfg);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaLaunchKernelEx(pass_kernel)");
+        if (gi > 0) {
+            e = cudaEventRecord(h->ev[gi], ls);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->ev[gi], 0);
+            if (e != cudaSuccess) return cuda_fail(h, e, "join side stream");
+        }
+        off += g.d.size();
     }
-    lc.attrs = attrs;
-    lc.numAttrs = na;
-    const PulseDev* dd = h->d_desc;
-    e = cudaLaunchKernelEx(&lc, ke->fn, dd, tabs, cfg);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaLaunchKernelEx(pass_kernel)");
     return OPTIFAX_OK;
+}
+
+int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, int C, int method,
+                 const VariantCfg& vc, bool shared, cudaStream_t st) {
+    std::vector<Group> groups(1);
+    groups[0].M = M;
+    groups[0].C = C;
+    groups[0].d = descs;
+    return launch_groups(h, groups, method, vc, shared, st);
 }
 
 bool is_pow2(long long x) { return x > 0 && (x & (x - 1)) == 0; }
@@ -315,6 +391,8 @@ int optifax_destroy(optifax_handle h) {
     if (h->d_desc) cudaFree(h->d_desc);
     if (h->d_grid_flags) cudaFree(h->d_grid_flags);
     if (h->d_xch) cudaFree(h->d_xch);
+    for (auto s_ : h->side) cudaStreamDestroy(s_);
+    for (auto e_ : h->ev) cudaEventDestroy(e_);
     delete h;
     return OPTIFAX_OK;
 }
@@ -355,19 +433,18 @@ int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_p
         PulseDev d;
         int rc = fill_desc(h, pulses[i], vc, &d, stats ? stats + i : nullptr);
         if (rc) return rc;
-        int M = choose_M(pulses[i].n_points, cta_points);
+        int want = pulses[i].cta_points > 0 ? pulses[i].cta_points : cta_points;
+        if (want != 0 && (!is_pow2(want) || want < 512 || want > 4096))
+            return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "pulse cta_points must be 0 or a power of two in [512, 4096]");
+        int M = choose_M(pulses[i].n_points, want);
         if (M > pulses[i].n_points) M = pulses[i].n_points;
         int C = pulses[i].n_points / M;
         if (C > 16) return fail(h, OPTIFAX_ERR_UNSUPPORTED, "n_points / cta_points exceeds 16");
         groups[{M, C}].push_back(d);
     }
-    // One launch per (M, C) group; a group's descriptors are staged in the
-    // context buffer, so groups are launched one after another on the stream.
-    for (auto& g : groups) {
-        int rc = launch_group(h, g.second, g.first.first, g.first.second, method, vc, false, st);
-        if (rc) return rc;
-    }
-    return OPTIFAX_OK;
+    std::vector<Group> gv;
+    for (auto& g : groups) gv.push_back(Group{g.first.first, g.first.second, std::move(g.second)});
+    return launch_groups(h, gv, method, vc, false, st);
 }
 
 int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cavities,
@@ -407,12 +484,9 @@ int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cav
         if (C > 16) return fail(h, OPTIFAX_ERR_UNSUPPORTED, "n_points / cta_points exceeds 16");
         groups[{M, C}].push_back(d);
     }
-    for (auto& g : groups) {
-        int rc = launch_group(h, g.second, g.first.first, g.first.second, OPTIFAX_HEUN, vc, false,
-                              (cudaStream_t)stream);
-        if (rc) return rc;
-    }
-    return OPTIFAX_OK;
+    std::vector<Group> gv;
+    for (auto& g : groups) gv.push_back(Group{g.first.first, g.first.second, std::move(g.second)});
+    return launch_groups(h, gv, OPTIFAX_HEUN, vc, false, (cudaStream_t)stream);
 }
 
 int optifax_opo_mex_batch(optifax_handle h,

@@ -114,6 +114,7 @@ class PulseSpec:
     trace_cap: int = 0
     forced: Optional[torch.Tensor] = None      # (n,) int32
     trace: Optional[torch.Tensor] = None       # filled: (trace_cap, 3) int32
+    cta_points: int = 0                        # points per CTA (0: the call's choice / autotuned)
 
 
 def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int = VARIANT_BATCH_XTAL,
@@ -154,6 +155,7 @@ def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int =
         d.bdiffw0, d.dt = float(p.bdiffw0), float(p.dt)
         d.max_err, d.min_err, d.sel = float(p.max_err), float(p.min_err), float(p.sel)
         d.stepmods_limit = 0
+        d.cta_points = int(p.cta_points or _tuned_cta_points(N, cta_points))
     stats = None
     if want_stats:
         stats = torch.zeros((len(pulses), nat.STATS_BYTES // 4), dtype=torch.int32, device=pulses[0].E.device)
@@ -162,6 +164,67 @@ def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int =
                                    _stream_ptr(stream))
     check(rc, ctx.handle, "optifax_propagate")
     return [p.out for p in pulses], stats
+
+
+# ---------------------------------------------------------------------------
+# Autotuner: points per CTA (and so cluster size) per grid size
+# ---------------------------------------------------------------------------
+_TUNED = {}
+
+
+def _tuned_cta_points(n_points: int, call_choice: int) -> int:
+    if call_choice:
+        return 0
+    return _TUNED.get(n_points, 0)
+
+
+def autotune(n_points_list=(4096, 8192, 16384, 32768, 65536), crystal_length=0.1e-3, replicas=None,
+             device: int = 0, verbose: bool = False) -> dict:
+    """Pick cta_points for each grid size by timing short crystal passes.
+
+    For each N every compiled cta_points in [max(512, N/16), min(4096, N)] is
+    timed on `replicas` identical pulses (default: enough to fill the GPU) and
+    the fastest per pulse-attempt is kept for later propagate() calls.
+    """
+    import time
+    from . import physics as ph
+    dev = torch.device(f"cuda:{device}")
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    out = {}
+    for N in n_points_list:
+        win = ph.SimWindow(1040e-9, N, N * 6e-12 / 2 ** 13)
+        si = ph.solver_inputs(ph.Crystal(crystal_length, 30e-6), win)
+        e = np.fft.fftshift(ph.sech_pump(win, 1040e-9, min(200e-15, win.temporal_range / 12), 2.0))
+        best = None
+        for M in (4096, 2048, 1024, 512):
+            if M > N or N // M > 16:
+                continue
+            reps = replicas or max(1, sms // (N // M))
+            mk = lambda: PulseSpec(E=torch.from_numpy(e.astype(np.complex64)).to(dev),
+                                   alpha=torch.from_numpy(si.alpha).to(dev), beta=torch.from_numpy(si.beta).to(dev),
+                                   G=torch.from_numpy(si.G).to(dev), w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                                   dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=si.sel,
+                                   n_steps=si.n_steps, cta_points=M)
+            specs = [mk() for _ in range(reps)]
+            try:
+                propagate(specs)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                _, st = propagate(specs)
+                torch.cuda.synchronize()
+                el = time.perf_counter() - t0
+            except Exception:
+                continue
+            att = sum(s_["attempts"] for s_ in decode_stats(st))
+            per = el / max(att, 1)
+            if verbose:
+                print(f"autotune N={N} cta_points={M}: {per * 1e6:.3f} us per pulse-attempt")
+            if best is None or per < best[1]:
+                best = (M, per)
+        if best:
+            out[N] = best[0]
+            _TUNED[N] = best[0]
+    return out
 
 
 def decode_stats(stats: torch.Tensor) -> List[dict]:

@@ -1,0 +1,69 @@
+"""Batched crystal-pass sweeps with uneven grids and crystals (BASELINE config 3).
+
+Every instance has its own grid size, crystal length, poling period, pump
+power and pulse width, and its own adaptive step schedule; all run in one
+optifax_propagate call (one grid per cluster shape, launched concurrently).
+The reference cannot batch these (one cuFFT plan and one shared step per MEX
+call, OPO_CUDA_BATCH_XTAL.cu:418-419,450-466), so it would run them one by one.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import List
+
+import numpy as np
+import torch
+
+from . import physics as ph
+from . import solver as sv
+
+DT = 6e-12 / 2 ** 13            # fixed sample spacing: window = N dt
+
+
+@dataclasses.dataclass
+class Instance:
+    n_points: int
+    length: float
+    period: float
+    power: float
+    tau: float
+    seed: int
+
+
+def config3_instances(n: int = 256, seed: int = 2, n_range=(12, 16), length_range=(0.5e-3, 10e-3),
+                      period_range=(28e-6, 32e-6), power_range=(0.5, 3.0), tau_range=(100e-15, 300e-15)):
+    """Instances drawn with a seeded generator: N uniform over 2^12..2^16 and the
+    other parameters uniform over their ranges."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(Instance(n_points=int(2 ** rng.integers(n_range[0], n_range[1] + 1)),
+                            length=float(rng.uniform(*length_range)),
+                            period=float(rng.uniform(*period_range)),
+                            power=float(rng.uniform(*power_range)),
+                            tau=float(rng.uniform(*tau_range)),
+                            seed=seed * 100000 + i))
+    return out
+
+
+def build_inputs(inst: Instance):
+    """Solver inputs and the in-crystal field (fftshifted, complex128) of one instance."""
+    win = ph.SimWindow(1040e-9, inst.n_points, inst.n_points * DT)
+    si = ph.solver_inputs(ph.Crystal(inst.length, inst.period), win)
+    pump = ph.sech_pump(win, 1040e-9, inst.tau, inst.power)
+    noise = ph.photon_noise(win, inst.seed, mask=ph.window_transmission(win))
+    e = np.fft.fftshift(pump + noise)
+    e = np.fft.ifft(np.fft.fft(e) * np.sqrt(1.0 / si.n_index))
+    return win, si, e
+
+
+def to_specs(inputs, device: int = 0, trace_cap: int = 0) -> List[sv.PulseSpec]:
+    dev = torch.device(f"cuda:{device}")
+    specs = []
+    for win, si, e in inputs:
+        specs.append(sv.PulseSpec(
+            E=torch.from_numpy(e.astype(np.complex64)).to(dev),
+            alpha=torch.from_numpy(si.alpha).to(dev), beta=torch.from_numpy(si.beta).to(dev),
+            G=torch.from_numpy(si.G).to(dev), w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, dt=si.dt,
+            max_err=si.max_err, min_err=si.min_err, sel=si.sel, n_steps=si.n_steps, trace_cap=trace_cap))
+    return specs

@@ -136,3 +136,29 @@ def test_mex_batch_shared_schedule(oracle):
     for b in range(B):
         assert rel_l2(A[b], ref.A[b]) <= FIELD_TOL
     assert np.array_equal(sm.cpu().numpy(), ref.stepmods.astype(np.float32))
+
+
+def test_uneven_batch_one_call(oracle):
+    """Pulses of different grid sizes, crystals and powers in one optifax_propagate
+    call (several cluster shapes launched together), each with its own step
+    schedule, each against its own oracle pass."""
+    import torch
+    from optifax_gb300 import sweep, solver as sv, _native as nat
+    insts = [sweep.Instance(1024, 0.15e-3, 29e-6, 1.0, 40e-15, 11),
+             sweep.Instance(2048, 0.10e-3, 31e-6, 2.5, 60e-15, 12),
+             sweep.Instance(4096, 0.20e-3, 30e-6, 0.8, 100e-15, 13),
+             sweep.Instance(8192, 0.05e-3, 28e-6, 3.0, 150e-15, 14),
+             sweep.Instance(1024, 0.30e-3, 32e-6, 2.0, 40e-15, 15),
+             sweep.Instance(4096, 0.05e-3, 30e-6, 1.5, 100e-15, 16)]
+    inputs = [sweep.build_inputs(i) for i in insts]
+    specs = sweep.to_specs(inputs, trace_cap=100000)
+    outs, stats = sv.propagate(specs)
+    torch.cuda.synchronize()
+    st = sv.decode_stats(stats)
+    for (win, si, e), o, spec, s_ in zip(inputs, outs, specs, st):
+        assert s_["status"] == 0
+        tr = spec.trace.cpu().numpy()[:s_["attempts"]]
+        ref = _oracle_pass(oracle, si, e, nat.HEUN, nat.VARIANT_BATCH_XTAL)
+        if not (len(ref.trace[0]) == len(tr) and np.array_equal(ref.trace[0][:, :2], tr[:, :2])):
+            ref = _oracle_pass(oracle, si, e, nat.HEUN, nat.VARIANT_BATCH_XTAL, forced=(tr[:, 2] & 3))
+        assert rel_l2(o.cpu().numpy(), ref.A[0]) <= FIELD_TOL
