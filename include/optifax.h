@@ -207,6 +207,30 @@ int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cav
 int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t variant,
                               optifax_pulse_stats* stats, void* stream);
 
+/*
+ * The plain full-FP64 crystal pass (Heun schedule of OPO_CUDA_BATCH_XTAL.cu:373-525
+ * and its BATCH_OP / NO_BC / HARD_BC variants, computed in double precision
+ * throughout, as the reference's FP64 MATLAB solver NEE_CPU.m computes it on the
+ * CPU).  It is the FP64 comparator of the FP32 propagator: one kernel per
+ * sub-operation over global memory and a host-side step decision after a flag
+ * read-back every attempt, like the reference's MEX driver.  The reference has no
+ * FP64 GPU entry point; this one takes the MEX argument list with double arrays.
+ *
+ * E_in, A_out: DEVICE arrays of n_pulses x n_points complex doubles (interleaved);
+ * alpha, beta: DEVICE, n_points doubles; G: DEVICE, n_steps doubles, or
+ * n_pulses x n_steps when g_per_pulse.  All pulses share one step schedule (the
+ * reference's batch rule).  trace_host (optional, HOST, 3 x trace_cap int32):
+ * per attempt {k, stepmod, flags | 8 if accepted}; stats_host (optional, HOST).
+ * Variant ODE23 is not offered.  Calls on one device are serialised internally.
+ */
+int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_t n_steps,
+                           const double* E_in, double* A_out, const double* alpha,
+                           const double* beta, const double* G, int32_t g_per_pulse,
+                           double w0, double bdiffw0, double step_h, double dt,
+                           double max_err, double min_err, double sel, int32_t variant,
+                           int32_t* trace_host, int32_t trace_cap,
+                           optifax_pulse_stats* stats_host, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

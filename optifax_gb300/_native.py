@@ -15,7 +15,8 @@ VARIANT_BATCH_XTAL, VARIANT_BATCH_OP, VARIANT_NO_BC, VARIANT_HARD_BC, VARIANT_OD
 PULSE_NAN, PULSE_ATTEMPT_LIMIT = 0x1, 0x2
 
 EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifax_last_error",
-           "optifax_opo_mex_batch", "optifax_propagate", "optifax_opo_run", "optifax_propagate_noalloc"]
+           "optifax_opo_mex_batch", "optifax_propagate", "optifax_opo_run", "optifax_propagate_noalloc",
+           "optifax_propagate_fp64"]
 
 _lib = None
 
@@ -75,6 +76,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_propagate.restype = ctypes.c_int
     lib.optifax_propagate_noalloc.argtypes = [ctypes.POINTER(OptifaxPulse), i32, vp, vp]
     lib.optifax_propagate_noalloc.restype = ctypes.c_int
+    lib.optifax_propagate_fp64.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, i32, f64, f64, f64, f64,
+                                           f64, f64, f64, i32, vp, i32, vp, vp]
+    lib.optifax_propagate_fp64.restype = ctypes.c_int
     _lib = lib
     return lib
 

@@ -1,0 +1,317 @@
+// ofx_fp64.cu -- the plain full-FP64 crystal-pass solver on the GPU.
+//
+// A straightforward double-precision implementation of the same schedule as
+// the reference driver (OPO_CUDA_BATCH_XTAL.cu:373-525): one kernel per
+// sub-operation over global memory, the step decision on the host after a
+// flag read-back each attempt, and this library's own radix-4 FFT (no cuFFT).
+// It is the FP64 comparator of the FP32 propagator (precision study,
+// BASELINE config 4) and the "plain FP64 solver" the OPO speed-up is measured
+// against.  GB300's FP64 rate is a small fraction of its FP32 rate; this
+// solver is not tuned beyond batching all pulses of a call in every launch.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/optifax.h"
+
+namespace {
+
+struct Fp64Work {
+    int n = 0, b = 0;
+    double2 *A0 = nullptr, *A1 = nullptr, *NL = nullptr, *K1 = nullptr, *T = nullptr;
+    double2* tw = nullptr;     // W_N^e, e < N/2
+    int* flags = nullptr;      // per call: bit0 >= maxErr, bit1 >= minErr, bit2 NaN
+    int* hflags = nullptr;     // pinned host copy
+};
+
+Fp64Work g_w[64];             // per device; a call allocates on first use or growth
+std::mutex g_mu[64];
+
+__device__ __forceinline__ double2 dmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ double sample_time(int mode, int i, int n, double dt) {
+    if (mode == 0) return (i > n / 2) ? dt * (double)(i - n / 2) : dt * (double)(i + n / 2);
+    return dt * (double)i;
+}
+
+// NL = A^2 e^{i phi} + 2 |A|^2 e^{-i phi}, phi = w0 t_i - bdwz
+__global__ void f64_nl(const double2* __restrict__ X, double2* __restrict__ NL, int n, double w0, double dt,
+                       double bdwz, int time_mode) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t o = (size_t)blockIdx.y * n + i;
+    double s, c;
+    sincos(w0 * sample_time(time_mode, i, n, dt) - bdwz, &s, &c);
+    double2 a = X[o];
+    double m2 = a.x * a.x + a.y * a.y;
+    double2 a2 = make_double2(a.x * a.x - a.y * a.y, 2.0 * a.x * a.y);
+    double2 e = make_double2(c, s);
+    double2 t = dmul(a2, e);
+    NL[o] = make_double2(t.x + 2.0 * m2 * c, t.y - 2.0 * m2 * s);
+}
+
+// K = -i hG (NL - i cs (NL[i+1] - NL[i-1])); mode 0: K1 = K, A1 = A0 + K;
+// mode 1: E = A0 + (K/2 + K1/2), class |E - (A0 + K1)| against the thresholds
+__global__ void f64_k(const double2* __restrict__ NL, const double2* __restrict__ A0, double2* __restrict__ K1,
+                      double2* __restrict__ X, const double* __restrict__ G, int gstride, int kidx, double hmod,
+                      double cs, int n, int mode, double maxE, double minE, int* flags) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int b = blockIdx.y;
+    size_t base = (size_t)b * n;
+    int ip = (i + 1 == n) ? 0 : i + 1, im = (i == 0) ? n - 1 : i - 1;
+    double2 d = make_double2(NL[base + ip].x - NL[base + im].x, NL[base + ip].y - NL[base + im].y);
+    double2 in = make_double2(NL[base + i].x + cs * d.y, NL[base + i].y - cs * d.x);
+    double hg = hmod * G[(size_t)kidx + (size_t)b * gstride];   // kidx clamped to [0, S) by the host
+    double2 k = make_double2(hg * in.y, -hg * in.x);
+    double2 a0 = A0[base + i];
+    if (mode == 0) {
+        K1[base + i] = k;
+        X[base + i] = make_double2(a0.x + (0.5 * k.x + 0.5 * k.x), a0.y + (0.5 * k.y + 0.5 * k.y));
+    } else {
+        double2 k1 = K1[base + i];
+        double2 e = make_double2(a0.x + (0.5 * k.x + 0.5 * k1.x), a0.y + (0.5 * k.y + 0.5 * k1.y));
+        double2 a1 = make_double2(a0.x + (0.5 * k1.x + 0.5 * k1.x), a0.y + (0.5 * k1.y + 0.5 * k1.y));
+        X[base + i] = e;
+        double ae = hypot(e.x, e.y);
+        int bits = 0;
+        if (ae > 0.0) {
+            double pct = 100.0 * hypot(e.x - a1.x, e.y - a1.y) / (ae + 1.0);
+            if (pct >= maxE) bits = 1;
+            else if (pct >= minE) bits = 2;
+        }
+        if (isnan(e.x) || isnan(e.y)) bits |= 4;
+        bits = __reduce_or_sync(__activemask(), bits);
+        if (bits && (threadIdx.x & 31) == 0) atomicOr(flags, bits);
+    }
+}
+
+__global__ void f64_abc(double2* X, int n, int abc_mode) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || abc_mode == 1) return;
+    int gi1 = 6 * (n / 16), gi2 = 10 * (n / 16);
+    if (!(i > gi1 && i < gi2)) return;
+    size_t o = (size_t)blockIdx.y * n + i;
+    double f;
+    if (abc_mode == 2) f = 0.0;
+    else {
+        double pos = (48.0 / (double)n) * fabs((double)i - (double)n / 2.0);
+        double g = cosh(pos);
+        f = 1.0 - 1.0 / (g * g);
+    }
+    X[o] = make_double2(X[o].x * f, X[o].y * f);
+}
+
+__global__ void f64_bitrev(const double2* __restrict__ x, double2* __restrict__ y, int n, int log2n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t base = (size_t)blockIdx.y * n;
+    int r = (int)(__brev((unsigned)i) >> (32 - log2n));
+    y[base + r] = x[base + i];
+}
+
+// two radix-2 DIT stages (len, 2 len) in place; `sign` +1 forward, -1 inverse
+__global__ void f64_radix4(double2* x, const double2* __restrict__ tw, int n, int len, int sign) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    int h = len / 2;
+    if (q >= n / 4) return;
+    int blk = q / h, j = q - blk * h;
+    size_t base = (size_t)blockIdx.y * n + (size_t)blk * 2 * len;
+    double2 w1 = tw[j * (n / len)];
+    double2 w2a = tw[j * (n / (2 * len))];
+    double2 w2b = tw[(j + h) * (n / (2 * len))];
+    if (sign < 0) { w1.y = -w1.y; w2a.y = -w2a.y; w2b.y = -w2b.y; }
+    double2 a = x[base + j], b = x[base + j + h], c = x[base + len + j], d = x[base + len + j + h];
+    double2 tb = dmul(b, w1), td = dmul(d, w1);
+    double2 a1 = make_double2(a.x + tb.x, a.y + tb.y), b1 = make_double2(a.x - tb.x, a.y - tb.y);
+    double2 c1 = make_double2(c.x + td.x, c.y + td.y), d1 = make_double2(c.x - td.x, c.y - td.y);
+    double2 tc = dmul(c1, w2a), tdd = dmul(d1, w2b);
+    x[base + j] = make_double2(a1.x + tc.x, a1.y + tc.y);
+    x[base + len + j] = make_double2(a1.x - tc.x, a1.y - tc.y);
+    x[base + j + h] = make_double2(b1.x + tdd.x, b1.y + tdd.y);
+    x[base + len + j + h] = make_double2(b1.x - tdd.x, b1.y - tdd.y);
+}
+
+__global__ void f64_radix2(double2* x, const double2* __restrict__ tw, int n, int len, int sign) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    int h = len / 2;
+    if (q >= n / 2) return;
+    int blk = q / h, j = q - blk * h;
+    size_t base = (size_t)blockIdx.y * n + (size_t)blk * len;
+    double2 w = tw[j * (n / len)];
+    if (sign < 0) w.y = -w.y;
+    double2 a = x[base + j], t = dmul(x[base + j + h], w);
+    x[base + j] = make_double2(a.x + t.x, a.y + t.y);
+    x[base + j + h] = make_double2(a.x - t.x, a.y - t.y);
+}
+
+__global__ void f64_twiddles(double2* tw, int n) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n / 2) return;
+    double s, c;
+    sincospi(-2.0 * (double)e / (double)n, &s, &c);
+    tw[e] = make_double2(c, s);
+}
+
+__global__ void f64_disp(double2* X, const double* __restrict__ alpha, const double* __restrict__ beta, int n,
+                         int s) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t o = (size_t)blockIdx.y * n + i;
+    double sn, cn;
+    sincos(-beta[i] * (double)s, &sn, &cn);
+    double a = pow(alpha[i], (double)s);
+    X[o] = dmul(X[o], make_double2(cn * a, sn * a));
+}
+
+__global__ void f64_scale(const double2* __restrict__ x, double2* __restrict__ y, int n, double sc) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    size_t o = (size_t)blockIdx.y * n + i;
+    y[o] = make_double2(x[o].x * sc, x[o].y * sc);
+}
+
+int ilog2i(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
+
+// forward (sign +1) or unnormalised inverse (sign -1) of every pulse, from src into dst
+void fft64(const double2* src, double2* dst, const double2* tw, int n, int b, int sign, cudaStream_t st) {
+    int lg = ilog2i(n);
+    dim3 grid((n + 255) / 256, b);
+    f64_bitrev<<<grid, 256, 0, st>>>(src, dst, n, lg);
+    int len = 2;
+    if (lg & 1) {
+        f64_radix2<<<dim3((n / 2 + 255) / 256, b), 256, 0, st>>>(dst, tw, n, 2, sign);
+        len = 4;
+    }
+    for (; len <= n / 2; len *= 4) f64_radix4<<<dim3((n / 4 + 255) / 256, b), 256, 0, st>>>(dst, tw, n, len, sign);
+}
+
+int ensure(Fp64Work& w, int n, int b) {
+    if (w.n == n && w.b >= b && w.A0) return 0;
+    for (double2* p : {w.A0, w.A1, w.NL, w.K1, w.T, w.tw}) if (p) cudaFree(p);
+    if (w.flags) cudaFree(w.flags);
+    if (w.hflags) cudaFreeHost(w.hflags);
+    w = Fp64Work();
+    size_t sz = sizeof(double2) * (size_t)n * b;
+    if (cudaMalloc(&w.A0, sz) || cudaMalloc(&w.A1, sz) || cudaMalloc(&w.NL, sz) || cudaMalloc(&w.K1, sz) ||
+        cudaMalloc(&w.T, sz) || cudaMalloc(&w.tw, sizeof(double2) * (size_t)(n / 2)) ||
+        cudaMalloc(&w.flags, sizeof(int)) || cudaMallocHost(&w.hflags, sizeof(int)))
+        return OPTIFAX_ERR_NO_MEMORY;
+    f64_twiddles<<<(n / 2 + 255) / 256, 256>>>(w.tw, n);
+    if (cudaDeviceSynchronize() != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    w.n = n;
+    w.b = b;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_t n_steps,
+                                      const double* E_in, double* A_out, const double* alpha, const double* beta,
+                                      const double* G, int32_t g_per_pulse, double w0, double bdiffw0,
+                                      double step_h, double dt, double max_err, double min_err, double sel,
+                                      int32_t variant, int32_t* trace_host, int32_t trace_cap,
+                                      optifax_pulse_stats* stats_host, void* stream) {
+    const int n = n_points, B = n_pulses, S = n_steps;
+    if (n < 16 || (n & (n - 1)) || B < 1 || S < 1 || !(sel >= 1.0) || !E_in || !A_out || !alpha || !beta || !G)
+        return OPTIFAX_ERR_INVALID_ARGUMENT;
+    int time_mode, abc_mode, guard;
+    switch (variant) {
+        case OPTIFAX_VARIANT_BATCH_XTAL:
+        case OPTIFAX_VARIANT_BATCH_OP: time_mode = 0; abc_mode = 0; guard = 1; break;
+        case OPTIFAX_VARIANT_NO_BC: time_mode = 1; abc_mode = 1; guard = 0; break;
+        case OPTIFAX_VARIANT_HARD_BC: time_mode = 1; abc_mode = 2; guard = 0; break;
+        default: return OPTIFAX_ERR_INVALID_ARGUMENT;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return OPTIFAX_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_mu[dev]);
+    Fp64Work& w = g_w[dev];
+    int rc = ensure(w, n, B);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t sz = sizeof(double2) * (size_t)n * B;
+    if (cudaMemcpyAsync(w.A0, E_in, sz, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    const dim3 grid((n + 255) / 256, B);
+    const double cs = 1.0 / (2.0 * dt * w0);
+    const int gstride = g_per_pulse ? S : 0;
+    int nchunks = (int)((double)S / sel);
+    if (guard && (double)nchunks * sel < (double)S) nchunks += 1;
+    double k = 0.0, stepprev = 4.0, stepmod = 4.0;
+    long long q = 0;
+    int attempt = 0, acc = 0, rej = 0, status = 0;
+    const long long max_attempts = 64LL * (S + 16) + 64;
+    for (int chunk = 0; chunk < nchunks; ++chunk) {
+        stepmod = stepprev;
+        const double cend = (double)(chunk + 1) * sel;
+        while (k < cend && (!guard || k < (double)S)) {
+            if (attempt >= max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; goto done; }
+            const int kidx = k < 0.0 ? 0 : ((int)k >= S ? S - 1 : (int)k);
+            const int krec = (int)k;
+            const double hmod = stepmod * step_h;
+            cudaMemsetAsync(w.flags, 0, sizeof(int), st);
+            f64_nl<<<grid, 256, 0, st>>>(w.A0, w.NL, n, w0, dt, bdiffw0 * k * step_h, time_mode);
+            f64_k<<<grid, 256, 0, st>>>(w.NL, w.A0, w.K1, w.A1, G, gstride, kidx, hmod, cs, n, 0, max_err, min_err,
+                                        w.flags);
+            f64_nl<<<grid, 256, 0, st>>>(w.A1, w.NL, n, w0, dt, bdiffw0 * (k + stepmod) * step_h, time_mode);
+            f64_k<<<grid, 256, 0, st>>>(w.NL, w.A0, w.K1, w.A1, G, gstride, kidx, hmod, cs, n, 1, max_err, min_err,
+                                        w.flags);
+            cudaMemcpyAsync(w.hflags, w.flags, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+            const int fl = *w.hflags;
+            if (fl & 4) status |= OPTIFAX_PULSE_NAN;
+            if ((fl & 1) && stepmod > 1.0 && (k - stepmod) > 0.0) {
+                if (trace_host && attempt < trace_cap) {
+                    trace_host[3 * attempt] = krec; trace_host[3 * attempt + 1] = (int)stepmod;
+                    trace_host[3 * attempt + 2] = fl & 7;
+                }
+                ++rej;
+                k = k - stepmod;
+                stepmod = stepmod - 1.0;
+                stepprev = stepmod;
+            } else {
+                if (trace_host && attempt < trace_cap) {
+                    trace_host[3 * attempt] = krec; trace_host[3 * attempt + 1] = (int)stepmod;
+                    trace_host[3 * attempt + 2] = (fl & 7) | 8;
+                }
+                ++acc;
+                const int s_used = (int)stepmod;
+                f64_abc<<<grid, 256, 0, st>>>(w.A1, n, abc_mode);
+                fft64(w.A1, w.T, w.tw, n, B, +1, st);
+                f64_disp<<<grid, 256, 0, st>>>(w.T, alpha, beta, n, s_used);
+                fft64(w.T, w.A1, w.tw, n, B, -1, st);
+                f64_scale<<<grid, 256, 0, st>>>(w.A1, w.A0, n, 1.0 / (double)n);
+                q += s_used;
+                if (k + stepmod >= cend && k < cend - 1.0) {
+                    double stepend = (cend - k) - 1.0;
+                    stepprev = stepmod;
+                    stepmod = stepend;
+                } else {
+                    if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.0) < cend - 1.0) stepmod = stepmod + 1.0;
+                    stepprev = stepmod;
+                }
+            }
+            ++attempt;
+            k = k + stepmod;
+        }
+    }
+done:
+    if (cudaMemcpyAsync(A_out, w.A0, sz, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    if (stats_host) {
+        memset(stats_host, 0, sizeof(*stats_host));
+        stats_host->attempts = attempt;
+        stats_host->accepted = acc;
+        stats_host->rejected = rej;
+        stats_host->status = status;
+        stats_host->z_steps = q;
+        stats_host->k_final = (float)k;
+        stats_host->stepmod_final = (float)stepmod;
+        stats_host->n_chunks = nchunks;
+    }
+    return OPTIFAX_OK;
+}

@@ -160,9 +160,15 @@ def qpm_signs(n_steps: int, length: float, period) -> np.ndarray:
     the crystal end).  ``period=("linear", p1, p2)`` gives an exact linear
     chirp of the local period from p1 at z=0 to p2 at z=L (walls where the
     accumulated QPM phase crosses multiples of pi).
+    ``period=("chirpedgrating", p1, p2, a, tol)`` takes the domain widths of
+    the reference's discretised power-law chirp (chirped_domain_widths).
     """
     z = np.linspace(0.0, length, n_steps)
-    if isinstance(period, (tuple, list)) and period[0] == "linear":
+    if isinstance(period, (tuple, list)) and period[0] == "chirpedgrating":
+        widths = chirped_domain_widths(z, *period[1:])
+        walls = np.cumsum(widths)
+        walls = walls[walls < length]      # a last domain past L is cut at L (QPMcrystal.m:44-50)
+    elif isinstance(period, (tuple, list)) and period[0] == "linear":
         p1, p2 = float(period[1]), float(period[2])
         a = (p2 - p1) / length
         theta_end = (np.log1p(a * length / p1) / a) if a != 0 else length / p1
@@ -178,6 +184,42 @@ def qpm_signs(n_steps: int, length: float, period) -> np.ndarray:
     q = np.searchsorted(edges, z, side="right")      # 1-based domain index
     q = np.mod(q, 2)
     return -(2.0 * q - 1.0)
+
+
+def chirped_domain_widths(z: np.ndarray, p1: float, p2: float, a: float = 1.0,
+                          tol: float = 0.1e-6) -> np.ndarray:
+    """Domain widths of a power-law chirped grating (chirpedgrating.m:1-47).
+
+    The local period p1 + (p2 - p1) (z/L)^a is quantised to multiples of tol
+    (p1 raised by tol and the grid offset by p2 + tol/2 before rounding, as
+    the reference does), halved to a domain width, and then sampled domain by
+    domain: each domain takes the width at the current z-sample and advances
+    by round(width / dz) samples, until the next domain would pass the end.
+    ``a = 1`` is a linear chirp.
+    """
+    z = np.asarray(z, dtype=np.float64)
+    p1 = p1 + tol
+    zfrac = z / z.max()
+    gr = p1 + (p2 - p1) * zfrac ** a - (p2 + tol / 2.0)
+    # MATLAB round(): half away from zero
+    q = np.sign(gr / tol) * np.floor(np.abs(gr / tol) + 0.5)
+    domains = q * tol / 2.0 + p2 / 2.0
+    dz = z[1] - z[0]
+    n_dom = int(np.ceil(np.sum(dz / domains)))
+    dsteps = np.sign(domains / dz) * np.floor(np.abs(domains / dz) + 0.5)
+    out = np.zeros(n_dom)
+    sid = 0                                  # 0-based stepID
+    pos = 0.0
+    zmax = z.max()
+    for ii in range(n_dom):
+        out[ii] = domains[sid]
+        sid = sid + int(dsteps[sid])
+        if sid > len(domains) - 1:
+            sid = len(domains) - 1
+        pos += out[ii]
+        if pos + domains[sid] > zmax:
+            return out[:ii + 1]
+    return out
 
 
 @dataclasses.dataclass

@@ -166,6 +166,44 @@ def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int =
     return [p.out for p in pulses], stats
 
 
+def propagate_fp64(E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
+                   variant: int = VARIANT_BATCH_XTAL, trace_cap: int = 0, stream=None):
+    """The plain full-FP64 crystal pass (optifax_propagate_fp64).
+
+    E: (B, N) or (N,) complex128 CUDA tensor; alpha, beta: (N,) float64; G: (S,)
+    or (B, S) float64.  Returns (A_out complex128 like E, stats dict, trace
+    ndarray (attempts, 3) or None).  All pulses share one schedule.
+    """
+    E = _cuda(E, torch.complex128)
+    squeeze = E.dim() == 1
+    if squeeze:
+        E = E.unsqueeze(0)
+    B, N = E.shape
+    al, be, G = _cuda(alpha, torch.float64), _cuda(beta, torch.float64), _cuda(G, torch.float64)
+    S = int(n_steps)
+    if al.numel() != N or be.numel() != N or G.numel() not in (S, S * B):
+        raise ValueError("alpha/beta must have N elements and G S or B*S")
+    g_per_pulse = int(G.numel() == S * B and B > 1)
+    out = torch.empty_like(E)
+    lib = nat.load()
+    st = nat.OptifaxPulseStats()
+    tr = (ctypes.c_int32 * (3 * trace_cap))() if trace_cap > 0 else None
+    if stream is None:
+        stream = torch.cuda.current_stream(E.device)
+    rc = lib.optifax_propagate_fp64(N, B, S, E.data_ptr(), out.data_ptr(), al.data_ptr(), be.data_ptr(),
+                                    G.data_ptr(), g_per_pulse, float(w0), float(bdiffw0), float(h), float(dt),
+                                    float(max_err), float(min_err), float(sel), int(variant),
+                                    ctypes.cast(tr, ctypes.c_void_p) if tr is not None else None,
+                                    int(trace_cap), ctypes.byref(st), int(stream.cuda_stream))
+    check(rc, None, "optifax_propagate_fp64")
+    stats = {f: getattr(st, f) for f, _ in nat.OptifaxPulseStats._fields_ if f != "reserved"}
+    trace = None
+    if tr is not None:
+        n = min(stats["attempts"], trace_cap)
+        trace = np.frombuffer(tr, dtype=np.int32).reshape(-1, 3)[:n].copy()
+    return (out[0] if squeeze else out), stats, trace
+
+
 # ---------------------------------------------------------------------------
 # Autotuner: points per CTA (and so cluster size) per grid size
 # ---------------------------------------------------------------------------
