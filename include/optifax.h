@@ -231,6 +231,24 @@ int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_t n_steps,
                            int32_t* trace_host, int32_t trace_cap,
                            optifax_pulse_stats* stats_host, void* stream);
 
+/*
+ * Surrogate-network building block: C[M, N] (+)= A[M, K] . B[N, K]^T on the tensor
+ * cores (tcgen05, TMA), A and B row-major BF16 DEVICE arrays with leading
+ * dimensions lda, ldb (elements, multiples of 8, base addresses 16-byte aligned),
+ * C row-major FP32 with leading dimension ldc.  a_rows >= max(M, 128) and
+ * b_rows >= max(N, 64) rows must be readable (the 128 x 64 and 64 x 64 tiles
+ * never read past them; rows past M or N may hold anything).  splits > 1 divides
+ * K over CTAs and adds the partial sums atomically; accumulate = 1 adds into C.
+ * No reference counterpart (the reference has no learned component).
+ */
+int optifax_gemm_bf16(const void* A, int64_t lda, int64_t a_rows, const void* B, int64_t ldb,
+                      int64_t b_rows, float* C, int64_t ldc, int32_t M, int32_t N, int32_t K,
+                      int32_t splits, int32_t accumulate, void* stream);
+
+/* Reads (and with clear != 0 resets) the tensor-core kernels' error flag: nonzero
+ * when a kernel gave up waiting for a copy or an MMA and skipped its output. */
+int optifax_tc_error(int32_t* out, int32_t clear);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,7 +46,7 @@ def build(case: PrecisionCase):
     return win, si, e
 
 
-def metrics(a: np.ndarray, ref: np.ndarray, floor: float = 1e-6) -> dict:
+def metrics(a: np.ndarray, ref: np.ndarray, floor: float = 1e-3) -> dict:
     """Field, energy and spectral-phase error of `a` against `ref` (same layout).
 
     The spectral phase error is the RMS of the wrapped phase difference per FFT
