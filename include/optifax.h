@@ -129,6 +129,7 @@ typedef struct {
     int32_t steady_tally;        /* tally index tested for flatness */
     float steady_tol;            /* |T_n - T_{n-1}| <= tol |T_n| counts as flat */
     int32_t reserved;
+    void* history;               /* optional: n_trips x N complex, crystal-output spectrum X of each trip */
 } optifax_opo;
 
 /* Create / destroy a context on a CUDA device.  The context owns the twiddle
@@ -248,6 +249,33 @@ int optifax_gemm_bf16(const void* A, int64_t lda, int64_t a_rows, const void* B,
 /* Reads (and with clear != 0 resets) the tensor-core kernels' error flag: nonzero
  * when a kernel gave up waiting for a copy or an MMA and skipped its output. */
 int optifax_tc_error(int32_t* out, int32_t clear);
+
+/*
+ * Fourier-neural-operator surrogate of one crystal pass (no reference
+ * counterpart).  Fixed architecture: 5 input channels (4 field channels + 1
+ * constant conditioning channel) over n_bins frequency bins, width 64, four
+ * spectral layers keeping 32 modes, GELU between layers, 4 output channels with a
+ * residual connection to the first 4 inputs.  Parameters are one FP32 vector of
+ * optifax_fno_param_count() values (layout in ofx_fno.cu); the kernels use BF16
+ * copies of the weights and BF16 activations with FP32 accumulation.
+ * x: DEVICE float [batch][5][n_bins]; y, target: DEVICE float [batch][4][n_bins].
+ * n_bins: a multiple of 64, >= 128.  One handle is used by one stream at a time.
+ */
+typedef struct optifax_fno_s* optifax_fno;
+int64_t optifax_fno_param_count(void);
+int optifax_fno_create(optifax_fno* out, int32_t n_bins, int32_t max_batch, int32_t device);
+int optifax_fno_destroy(optifax_fno f);
+/* copy params (DEVICE, FP32) into the network; resets the Adam moments */
+int optifax_fno_set_params(optifax_fno f, const float* params, void* stream);
+int optifax_fno_get_params(optifax_fno f, float* params, void* stream);
+int optifax_fno_forward(optifax_fno f, const float* x, float* y, int32_t batch, void* stream);
+/* forward + backward of loss = mean((y - target)^2); loss (DEVICE scalar) and grads
+ * (DEVICE, param_count floats) are optional copies of the results */
+int optifax_fno_backward(optifax_fno f, const float* x, const float* target, int32_t batch,
+                         float* loss, float* grads, void* stream);
+/* AdamW step (decoupled weight decay) with the gradients of the last backward; step >= 1 */
+int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta2, float eps,
+                     float weight_decay, int32_t step, void* stream);
 
 #ifdef __cplusplus
 }

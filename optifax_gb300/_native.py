@@ -16,7 +16,9 @@ PULSE_NAN, PULSE_ATTEMPT_LIMIT = 0x1, 0x2
 
 EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifax_last_error",
            "optifax_opo_mex_batch", "optifax_propagate", "optifax_opo_run", "optifax_propagate_noalloc",
-           "optifax_propagate_fp64", "optifax_gemm_bf16", "optifax_tc_error"]
+           "optifax_propagate_fp64", "optifax_gemm_bf16", "optifax_tc_error",
+           "optifax_fno_param_count", "optifax_fno_create", "optifax_fno_destroy", "optifax_fno_set_params",
+           "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam"]
 
 _lib = None
 
@@ -84,6 +86,22 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_gemm_bf16.restype = ctypes.c_int
     lib.optifax_tc_error.argtypes = [ctypes.POINTER(i32), i32]
     lib.optifax_tc_error.restype = ctypes.c_int
+    lib.optifax_fno_param_count.argtypes = []
+    lib.optifax_fno_param_count.restype = ctypes.c_int64
+    lib.optifax_fno_create.argtypes = [ctypes.POINTER(vp), i32, i32, i32]
+    lib.optifax_fno_create.restype = ctypes.c_int
+    lib.optifax_fno_destroy.argtypes = [vp]
+    lib.optifax_fno_destroy.restype = ctypes.c_int
+    lib.optifax_fno_set_params.argtypes = [vp, vp, vp]
+    lib.optifax_fno_set_params.restype = ctypes.c_int
+    lib.optifax_fno_get_params.argtypes = [vp, vp, vp]
+    lib.optifax_fno_get_params.restype = ctypes.c_int
+    lib.optifax_fno_forward.argtypes = [vp, vp, vp, i32, vp]
+    lib.optifax_fno_forward.restype = ctypes.c_int
+    lib.optifax_fno_backward.argtypes = [vp, vp, vp, i32, vp, vp, vp]
+    lib.optifax_fno_backward.restype = ctypes.c_int
+    lib.optifax_fno_adam.argtypes = [vp, f32, f32, f32, f32, f32, i32, vp]
+    lib.optifax_fno_adam.restype = ctypes.c_int
     _lib = lib
     return lib
 

@@ -478,6 +478,7 @@ int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cav
         d.steady_trips = cv.steady_trips;
         d.steady_tally = cv.steady_tally;
         d.steady_tol = cv.steady_tol;
+        d.hist = (float2*)cv.history;
         int M = choose_M(cv.pass.n_points, cta_points);
         if (M > cv.pass.n_points) M = cv.pass.n_points;
         int C = cv.pass.n_points / M;

@@ -1,0 +1,645 @@
+// ofx_fno.cu -- Fourier-neural-operator surrogate of one crystal pass: forward,
+// backward and AdamW on the GPU.  No reference counterpart (the reference has no
+// learned component).
+//
+// Network (fixed sizes): input x[b][5][L] (4 field channels and one constant
+// conditioning channel over L frequency bins), lifting to width 64, four Fourier
+// layers h <- act(SpecConv(h) + Wp h + bias) with 32 retained modes (no activation
+// after the last), projection to 4 channels plus a residual connection to the
+// first 4 input channels: y = x[:4] + Q h + q.
+//
+// Data layouts (per batch of B samples): "channel-major" Hc[c][b][x] and
+// "point-major" Ht[b][x][c] copies of every activation, so that every product is
+// an A . B^T GEMM with both operands K-major for the tensor-core kernel
+// (optifax_gemm_bf16):
+//   spectral transform   S[(c,b)][m'] = Hc . F^T         (F: 64 x L, m' = 2m + re/im)
+//   inverse transform    Y1[(o,b)][x] = T . G^T          (G: L x 64)
+//   pointwise mix        Y2[(b,x)][o] = Ht . Wp^T        (Wp: 64 x 64, [o][c])
+//   weight gradient      dWp[o][c]    = dZc[o][(b,x)] . Hc[c][(b,x)]^T
+//   backward transforms  dT = dZc . GT^T, dHs = dS . FT^T, dHp = dZt . WpT^T
+// The per-mode complex channel mixing T[(o,b)][m] = sum_c S[(c,b)][m] W[c][o][m]
+// and the element-wise parts run on the CUDA cores.  GEMM operands and
+// activations are BF16; accumulation, pre-activations, gradients, biases, the
+// master weights and the Adam moments are FP32.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#include "../../include/optifax.h"
+
+typedef __nv_bfloat16 bf16;
+
+namespace {
+
+constexpr int W = 64, MODES = 32, NLAYER = 4, CIN = 5, COUT = 4, SPEC = 2 * MODES;
+constexpr long long LAYER_WS = (long long)W * W * MODES * 2;   // [c][o][m][re,im]
+constexpr long long LAYER_SIZE = LAYER_WS + W * W + W;         // Ws, Wp [o][c], bias [o]
+constexpr long long OFF_P = 0;                                 // [W][CIN]
+constexpr long long OFF_PB = OFF_P + W * CIN;                  // [W]
+constexpr long long OFF_L0 = OFF_PB + W;
+constexpr long long OFF_Q = OFF_L0 + NLAYER * LAYER_SIZE;      // [COUT][W]
+constexpr long long OFF_QB = OFF_Q + COUT * W;                 // [COUT]
+constexpr long long N_PARAMS = OFF_QB + COUT;
+constexpr long long off_ws(int l) { return OFF_L0 + l * LAYER_SIZE; }
+constexpr long long off_wp(int l) { return off_ws(l) + LAYER_WS; }
+constexpr long long off_b(int l) { return off_wp(l) + W * W; }
+static_assert(off_wp(0) % 8 == 0 && LAYER_SIZE % 8 == 0, "BF16 GEMM operands must stay 16-byte aligned");
+
+constexpr int XT = 4;   // 32-point x tiles per block in the transposing kernels
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_d(float z) {
+    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
+
+// ---- tables --------------------------------------------------------------
+__global__ void k_dft_tables(int L, bf16* F, bf16* FT, bf16* G, bf16* GT) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)SPEC * L) return;
+    const int mp = (int)(i / L), x = (int)(i % L), m = mp >> 1;
+    const long long ph = ((long long)m * x) % L;
+    float s, c;
+    sincospif(2.f * (float)ph / (float)L, &s, &c);
+    const float f = (mp & 1) ? -s : c;
+    const float g = f * (m == 0 ? 1.f : 2.f) / (float)L;
+    F[(long long)mp * L + x] = __float2bfloat16(f);
+    FT[(long long)x * SPEC + mp] = __float2bfloat16(f);
+    G[(long long)x * SPEC + mp] = __float2bfloat16(g);
+    GT[(long long)mp * L + x] = __float2bfloat16(g);
+}
+
+__global__ void k_refresh(const float* __restrict__ master, bf16* wb, bf16* wpt) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < N_PARAMS) wb[i] = __float2bfloat16(master[i]);
+    if (i < (long long)NLAYER * W * W) {
+        const int l = (int)(i / (W * W)), r = (int)(i % (W * W)), c = r / W, o = r % W;
+        wpt[i] = __float2bfloat16(master[off_wp(l) + (long long)o * W + c]);
+    }
+}
+
+// ---- forward -------------------------------------------------------------
+__global__ void k_lift(const float* __restrict__ x, const bf16* __restrict__ Pw, const float* __restrict__ pb, int B,
+                       int L, bf16* __restrict__ Hc, bf16* __restrict__ Ht) {
+    __shared__ float sP[W * CIN];
+    __shared__ float sb[W];
+    for (int i = threadIdx.x; i < W * CIN; i += blockDim.x) sP[i] = __bfloat162float(Pw[i]);
+    for (int i = threadIdx.x; i < W; i += blockDim.x) sb[i] = pb[i];
+    __syncthreads();
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * L) return;
+    const int b = (int)(idx / L), xx = (int)(idx % L);
+    float in[CIN];
+#pragma unroll
+    for (int i = 0; i < CIN; ++i) in[i] = x[((long long)b * CIN + i) * L + xx];
+    uint4 pack[W / 8];
+    bf16* hp = reinterpret_cast<bf16*>(pack);
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+        float h = sb[c];
+#pragma unroll
+        for (int i = 0; i < CIN; ++i) h = fmaf(sP[c * CIN + i], in[i], h);
+        const bf16 hb = __float2bfloat16(h);
+        hp[c] = hb;
+        Hc[((long long)c * B + b) * L + xx] = hb;
+    }
+    uint4* dst = reinterpret_cast<uint4*>(Ht + idx * W);
+#pragma unroll
+    for (int j = 0; j < W / 8; ++j) dst[j] = pack[j];
+}
+
+// T[(o,b)][m] = sum_c S[(c,b)][m] W[c][o][m]   (complex)
+__global__ void k_mix_fwd(const float* __restrict__ S, const bf16* __restrict__ Ws, int B, bf16* __restrict__ T) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)W * B * MODES) return;
+    const int m = (int)(idx % MODES);
+    const long long t = idx / MODES;
+    const int b = (int)(t % B), o = (int)(t / B);
+    float ar = 0.f, ai = 0.f;
+    for (int c = 0; c < W; ++c) {
+        const float* s = S + ((long long)c * B + b) * SPEC + 2 * m;
+        const __nv_bfloat162 w = *reinterpret_cast<const __nv_bfloat162*>(Ws + (((long long)c * W + o) * MODES + m) * 2);
+        const float wr = __low2float(w), wi = __high2float(w);
+        ar = fmaf(s[0], wr, fmaf(-s[1], wi, ar));
+        ai = fmaf(s[0], wi, fmaf(s[1], wr, ai));
+    }
+    bf16* d = T + ((long long)o * B + b) * SPEC + 2 * m;
+    d[0] = __float2bfloat16(ar);
+    d[1] = __float2bfloat16(ai);
+}
+
+// Z = Y1[c][b][x] + Y2[b][x][c] + bias[c]; h = act(Z) -> Hc, Ht (and Z kept for the backward)
+__global__ void k_combine_fwd(const float* __restrict__ Y1, const float* __restrict__ Y2, const float* __restrict__ bias,
+                              int B, int L, int act, float* __restrict__ Zs, bf16* __restrict__ Hc,
+                              bf16* __restrict__ Ht) {
+    __shared__ float tile[32][W + 1];
+    const int b = blockIdx.y;
+    for (int xt = 0; xt < XT; ++xt) {
+        const int x0 = (blockIdx.x * XT + xt) * 32;
+        if (x0 >= L) break;
+        for (int r = 0; r < 8; ++r) {
+            const int i = threadIdx.x + 256 * r, xi = i / W, c = i % W;
+            tile[xi][c] = Y2[((long long)b * L + x0 + xi) * W + c];
+        }
+        __syncthreads();
+        float hv[8];
+        for (int r = 0; r < 8; ++r) {
+            const int i = threadIdx.x + 256 * r, c = i / 32, xi = i % 32;
+            const long long o = ((long long)c * B + b) * L + x0 + xi;
+            const float z = Y1[o] + tile[xi][c] + bias[c];
+            if (Zs) Zs[o] = z;
+            const float h = act ? gelu(z) : z;
+            Hc[o] = __float2bfloat16(h);
+            hv[r] = h;
+        }
+        __syncthreads();
+        for (int r = 0; r < 8; ++r) {
+            const int i = threadIdx.x + 256 * r, c = i / 32, xi = i % 32;
+            tile[xi][c] = hv[r];
+        }
+        __syncthreads();
+        for (int r = 0; r < 8; ++r) {
+            const int i = threadIdx.x + 256 * r, xi = i / W, c = i % W;
+            Ht[((long long)b * L + x0 + xi) * W + c] = __float2bfloat16(tile[xi][c]);
+        }
+        __syncthreads();
+    }
+}
+
+// y[b][j][x] = x[b][j][x] + q[j] + sum_c Q[j][c] h[b][x][c]
+__global__ void k_proj_fwd(const bf16* __restrict__ Ht, const bf16* __restrict__ Qw, const float* __restrict__ qb,
+                           const float* __restrict__ xin, int B, int L, float* __restrict__ y) {
+    __shared__ float sQ[COUT * W];
+    for (int i = threadIdx.x; i < COUT * W; i += blockDim.x) sQ[i] = __bfloat162float(Qw[i]);
+    __syncthreads();
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)B * L) return;
+    const int b = (int)(idx / L), xx = (int)(idx % L);
+    float acc[COUT];
+#pragma unroll
+    for (int j = 0; j < COUT; ++j) acc[j] = qb[j];
+    const uint4* src = reinterpret_cast<const uint4*>(Ht + idx * W);
+#pragma unroll
+    for (int q8 = 0; q8 < W / 8; ++q8) {
+        const uint4 u = src[q8];
+        const bf16* hp = reinterpret_cast<const bf16*>(&u);
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const float h = __bfloat162float(hp[e]);
+#pragma unroll
+            for (int j = 0; j < COUT; ++j) acc[j] = fmaf(sQ[j * W + q8 * 8 + e], h, acc[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < COUT; ++j)
+        y[((long long)b * COUT + j) * L + xx] = xin[((long long)b * CIN + j) * L + xx] + acc[j];
+}
+
+// ---- loss and backward ---------------------------------------------------
+__global__ void k_loss(const float* __restrict__ y, const float* __restrict__ t, long long n, float inv_n,
+                       float* __restrict__ dy, float* __restrict__ loss) {
+    __shared__ float red[32];
+    float part = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float d = y[i] - t[i];
+        dy[i] = 2.f * d * inv_n;
+        part = fmaf(d, d, part);
+    }
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) atomicAdd(loss, v * inv_n);
+    }
+}
+
+// dH4 = Q^T dy (the last layer has no activation, so this is dZ of layer 3) -> dZc, dZt; bias grad
+__global__ void k_proj_bwd(const float* __restrict__ dy, const bf16* __restrict__ Qw, int B, int L,
+                           bf16* __restrict__ dZc, bf16* __restrict__ dZt, float* __restrict__ db) {
+    __shared__ float sQ[COUT * W];
+    __shared__ float sdb[W];
+    for (int i = threadIdx.x; i < COUT * W; i += blockDim.x) sQ[i] = __bfloat162float(Qw[i]);
+    for (int i = threadIdx.x; i < W; i += blockDim.x) sdb[i] = 0.f;
+    __syncthreads();
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool live = idx < (long long)B * L;
+    float d[COUT] = {0.f, 0.f, 0.f, 0.f};
+    int b = 0, xx = 0;
+    if (live) {
+        b = (int)(idx / L);
+        xx = (int)(idx % L);
+#pragma unroll
+        for (int j = 0; j < COUT; ++j) d[j] = dy[((long long)b * COUT + j) * L + xx];
+    }
+    uint4 pack[W / 8];
+    bf16* gp = reinterpret_cast<bf16*>(pack);
+#pragma unroll
+    for (int c = 0; c < W; ++c) {
+        float g = 0.f;
+#pragma unroll
+        for (int j = 0; j < COUT; ++j) g = fmaf(sQ[j * W + c], d[j], g);
+        gp[c] = __float2bfloat16(g);
+        if (live) dZc[((long long)c * B + b) * L + xx] = gp[c];
+        float s = g;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&sdb[c], s);
+    }
+    if (live) {
+        uint4* dst = reinterpret_cast<uint4*>(dZt + idx * W);
+#pragma unroll
+        for (int j = 0; j < W / 8; ++j) dst[j] = pack[j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < W; i += blockDim.x) atomicAdd(&db[i], sdb[i]);
+}
+
+// dQ[j][c] = sum_(b,x) dy[b][j][x] h[b][x][c];  dq[j] = sum dy[b][j][x]
+__global__ void k_proj_wgrad(const float* __restrict__ dy, const bf16* __restrict__ Ht, int B, int L, int rows_per_block,
+                             float* __restrict__ dQ, float* __restrict__ dq) {
+    __shared__ float hs[64][W + 1];
+    __shared__ float ds[COUT][64];
+    const int t = threadIdx.x, j = t / W, c = t % W;
+    const long long total = (long long)B * L;
+    const long long r0 = (long long)blockIdx.x * rows_per_block;
+    float acc = 0.f, accq = 0.f;
+    for (long long base = r0; base < r0 + rows_per_block && base < total; base += 64) {
+        for (int r = 0; r < 16; ++r) {
+            const int i = t + 256 * r, row = i / W, cc = i % W;
+            const long long g = base + row;
+            hs[row][cc] = g < total ? __bfloat162float(Ht[g * W + cc]) : 0.f;
+        }
+        {
+            const int jj = t / 64, rr = t % 64;
+            const long long g = base + rr;
+            ds[jj][rr] = g < total ? dy[((g / L) * COUT + jj) * L + (g % L)] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int rr = 0; rr < 64; ++rr) acc = fmaf(ds[j][rr], hs[rr][c], acc);
+        if (c == 0)
+            for (int rr = 0; rr < 64; ++rr) accq += ds[j][rr];
+        __syncthreads();
+    }
+    atomicAdd(&dQ[j * W + c], acc);
+    if (c == 0) atomicAdd(&dq[j], accq);
+}
+
+// dS[(c,b)][m] = sum_o dT[(o,b)][m] conj(W[c][o][m])
+__global__ void k_mix_bwd_ds(const float* __restrict__ dT, const bf16* __restrict__ Ws, int B, bf16* __restrict__ dS) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)W * B * MODES) return;
+    const int m = (int)(idx % MODES);
+    const long long t = idx / MODES;
+    const int b = (int)(t % B), c = (int)(t / B);
+    float ar = 0.f, ai = 0.f;
+    for (int o = 0; o < W; ++o) {
+        const float* d = dT + ((long long)o * B + b) * SPEC + 2 * m;
+        const __nv_bfloat162 w = *reinterpret_cast<const __nv_bfloat162*>(Ws + (((long long)c * W + o) * MODES + m) * 2);
+        const float wr = __low2float(w), wi = __high2float(w);
+        ar = fmaf(d[0], wr, fmaf(d[1], wi, ar));
+        ai = fmaf(d[1], wr, fmaf(-d[0], wi, ai));
+    }
+    bf16* o_ = dS + ((long long)c * B + b) * SPEC + 2 * m;
+    o_[0] = __float2bfloat16(ar);
+    o_[1] = __float2bfloat16(ai);
+}
+
+// dW[c][o][m] = sum_b conj(S[(c,b)][m]) dT[(o,b)][m]
+__global__ void k_mix_bwd_dw(const float* __restrict__ dT, const float* __restrict__ S, int B, float* __restrict__ dW) {
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)W * W * MODES) return;
+    const int m = (int)(idx % MODES);
+    const long long t = idx / MODES;
+    const int o = (int)(t % W), c = (int)(t / W);
+    float ar = 0.f, ai = 0.f;
+    for (int b = 0; b < B; ++b) {
+        const float* s = S + ((long long)c * B + b) * SPEC + 2 * m;
+        const float* d = dT + ((long long)o * B + b) * SPEC + 2 * m;
+        ar = fmaf(s[0], d[0], fmaf(s[1], d[1], ar));
+        ai = fmaf(s[0], d[1], fmaf(-s[1], d[0], ai));
+    }
+    dW[(((long long)c * W + o) * MODES + m) * 2] = ar;
+    dW[(((long long)c * W + o) * MODES + m) * 2 + 1] = ai;
+}
+
+// g = dHs[c][b][x] + dHp[b][x][c]; with Zprev: dZ = g act'(Zprev) -> dZc, dZt, bias grad;
+// without (layer 0): g written back into dHs (the gradient of the lifted input)
+__global__ void k_combine_bwd(float* __restrict__ dHs, const float* __restrict__ dHp, const float* __restrict__ Zprev,
+                              int B, int L, bf16* __restrict__ dZc, bf16* __restrict__ dZt, float* __restrict__ db) {
+    __shared__ float tile[32][W + 1];
+    const int b = blockIdx.y;
+    float bsum[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int xt = 0; xt < XT; ++xt) {
+        const int x0 = (blockIdx.x * XT + xt) * 32;
+        if (x0 >= L) break;
+        for (int r = 0; r < 8; ++r) {
+            const int i = threadIdx.x + 256 * r, xi = i / W, c = i % W;
+            tile[xi][c] = dHp[((long long)b * L + x0 + xi) * W + c];
+        }
+        __syncthreads();
+        float gv[8];
+        for (int r = 0; r < 8; ++r) {
+            const int i = threadIdx.x + 256 * r, c = i / 32, xi = i % 32;
+            const long long o = ((long long)c * B + b) * L + x0 + xi;
+            float g = dHs[o] + tile[xi][c];
+            if (Zprev) {
+                g *= gelu_d(Zprev[o]);
+                dZc[o] = __float2bfloat16(g);
+                bsum[r] += g;
+            } else {
+                dHs[o] = g;
+            }
+            gv[r] = g;
+        }
+        __syncthreads();
+        if (Zprev) {
+            for (int r = 0; r < 8; ++r) {
+                const int i = threadIdx.x + 256 * r, c = i / 32, xi = i % 32;
+                tile[xi][c] = gv[r];
+            }
+            __syncthreads();
+            for (int r = 0; r < 8; ++r) {
+                const int i = threadIdx.x + 256 * r, xi = i / W, c = i % W;
+                dZt[((long long)b * L + x0 + xi) * W + c] = __float2bfloat16(tile[xi][c]);
+            }
+            __syncthreads();
+        }
+    }
+    if (Zprev) {
+        // every warp holds channels warp + 8 r (r = 0..7) across its 32 lanes
+        for (int r = 0; r < 8; ++r) {
+            float s = bsum[r];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if ((threadIdx.x & 31) == 0) atomicAdd(&db[(threadIdx.x >> 5) + 8 * r], s);
+        }
+    }
+}
+
+// dP[c][i] = sum_(b,x) dH0[c][b][x] x[b][i][x];  dp[c] = sum dH0[c][b][x]
+__global__ void k_lift_wgrad(const float* __restrict__ dH0, const float* __restrict__ x, int B, int L,
+                             float* __restrict__ dP, float* __restrict__ dp) {
+    __shared__ float red[CIN + 1][8];
+    const int c = blockIdx.x;
+    const long long total = (long long)B * L;
+    float acc[CIN + 1];
+#pragma unroll
+    for (int i = 0; i <= CIN; ++i) acc[i] = 0.f;
+    for (long long g = blockIdx.y * (long long)blockDim.x + threadIdx.x; g < total;
+         g += (long long)gridDim.y * blockDim.x) {
+        const int b = (int)(g / L), xx = (int)(g % L);
+        const float d = dH0[((long long)c * B + b) * L + xx];
+        acc[CIN] += d;
+#pragma unroll
+        for (int i = 0; i < CIN; ++i) acc[i] = fmaf(d, x[((long long)b * CIN + i) * L + xx], acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i <= CIN; ++i) {
+        float s = acc[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x <= CIN) {
+        float s = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+        if (threadIdx.x < CIN) atomicAdd(&dP[c * CIN + threadIdx.x], s);
+        else atomicAdd(&dp[c], s);
+    }
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       long long n, float lr, float b1, float b2, float eps, float wd, float bc1, float bc2) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * ((mi / bc1) / (sqrtf(vi / bc2) + eps) + wd * p[i]);
+}
+
+inline unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+struct optifax_fno_s {
+    int device = 0, L = 0, maxB = 0;
+    float *master = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    bf16 *wb = nullptr, *wpt = nullptr;
+    bf16 *F = nullptr, *FT = nullptr, *G = nullptr, *GT = nullptr;
+    bf16 *Hc[NLAYER + 1] = {}, *Ht[NLAYER + 1] = {};
+    float* Z[NLAYER - 1] = {};
+    float* S[NLAYER] = {};
+    bf16 *T = nullptr, *dS = nullptr, *dZc = nullptr, *dZt = nullptr;
+    float *Y1 = nullptr, *Y2 = nullptr, *y = nullptr, *dy = nullptr, *dT = nullptr, *loss = nullptr;
+};
+
+namespace {
+
+template <typename P>
+int alloc0(P** p, size_t bytes) {
+    if (cudaMalloc(reinterpret_cast<void**>(p), bytes) != cudaSuccess) return OPTIFAX_ERR_NO_MEMORY;
+    if (cudaMemset(*p, 0, bytes) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    return OPTIFAX_OK;
+}
+
+#define OFX_TRY(x)                    \
+    do {                              \
+        int rc_ = (x);                \
+        if (rc_) return rc_;          \
+    } while (0)
+
+int fno_forward(optifax_fno_s* f, const float* x, int B, cudaStream_t st) {
+    const int L = f->L;
+    const long long WB = (long long)W * B, rowsA = WB > 128 ? WB : 128;
+    k_lift<<<nblk((long long)B * L), 256, 0, st>>>(x, f->wb + OFF_P, f->master + OFF_PB, B, L, f->Hc[0], f->Ht[0]);
+    for (int l = 0; l < NLAYER; ++l) {
+        OFX_TRY(optifax_gemm_bf16(f->Hc[l], L, rowsA, f->F, L, SPEC, f->S[l], SPEC, (int)WB, SPEC, L, 8, 0, st));
+        k_mix_fwd<<<nblk(WB * MODES), 256, 0, st>>>(f->S[l], f->wb + off_ws(l), B, f->T);
+        OFX_TRY(optifax_gemm_bf16(f->T, SPEC, rowsA, f->G, SPEC, L, f->Y1, L, (int)WB, L, SPEC, 1, 0, st));
+        OFX_TRY(optifax_gemm_bf16(f->Ht[l], W, (long long)B * L, f->wb + off_wp(l), W, W, f->Y2, W, B * L, W, W, 1,
+                                  0, st));
+        const int act = l < NLAYER - 1;
+        k_combine_fwd<<<dim3((L + 32 * XT - 1) / (32 * XT), B), 256, 0, st>>>(
+            f->Y1, f->Y2, f->master + off_b(l), B, L, act, act ? f->Z[l] : nullptr, f->Hc[l + 1], f->Ht[l + 1]);
+    }
+    k_proj_fwd<<<nblk((long long)B * L), 256, 0, st>>>(f->Ht[NLAYER], f->wb + OFF_Q, f->master + OFF_QB, x, B, L,
+                                                       f->y);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+int fno_backward(optifax_fno_s* f, const float* x, const float* target, int B, cudaStream_t st) {
+    const int L = f->L;
+    const long long WB = (long long)W * B, rowsA = WB > 128 ? WB : 128, BL = (long long)B * L;
+    if (cudaMemsetAsync(f->grad, 0, sizeof(float) * N_PARAMS, st) != cudaSuccess ||
+        cudaMemsetAsync(f->loss, 0, sizeof(float), st) != cudaSuccess)
+        return OPTIFAX_ERR_CUDA;
+    const long long ny = BL * COUT;
+    k_loss<<<256, 256, 0, st>>>(f->y, target, ny, 1.f / (float)ny, f->dy, f->loss);
+    k_proj_bwd<<<nblk(BL), 256, 0, st>>>(f->dy, f->wb + OFF_Q, B, L, f->dZc, f->dZt, f->grad + off_b(NLAYER - 1));
+    const int rpb = 2048;
+    k_proj_wgrad<<<nblk(BL, rpb), 256, 0, st>>>(f->dy, f->Ht[NLAYER], B, L, rpb, f->grad + OFF_Q, f->grad + OFF_QB);
+    for (int l = NLAYER - 1; l >= 0; --l) {
+        const int splits = (int)((BL + 2047) / 2048);
+        OFX_TRY(optifax_gemm_bf16(f->dZc, BL, 128, f->Hc[l], BL, W, f->grad + off_wp(l), W, W, W, (int)BL, splits, 1,
+                                  st));
+        OFX_TRY(optifax_gemm_bf16(f->dZc, L, 2 * WB, f->GT, L, SPEC, f->dT, SPEC, (int)WB, SPEC, L, 8, 0, st));
+        k_mix_bwd_ds<<<nblk(WB * MODES), 256, 0, st>>>(f->dT, f->wb + off_ws(l), B, f->dS);
+        k_mix_bwd_dw<<<nblk((long long)W * W * MODES), 256, 0, st>>>(f->dT, f->S[l], B, f->grad + off_ws(l));
+        OFX_TRY(optifax_gemm_bf16(f->dS, SPEC, rowsA, f->FT, SPEC, L, f->Y1, L, (int)WB, L, SPEC, 1, 0, st));
+        OFX_TRY(optifax_gemm_bf16(f->dZt, W, BL, f->wpt + (long long)l * W * W, W, W, f->Y2, W, (int)BL, W, W, 1, 0,
+                                  st));
+        const dim3 cg((L + 32 * XT - 1) / (32 * XT), B);
+        if (l > 0) {
+            k_combine_bwd<<<cg, 256, 0, st>>>(f->Y1, f->Y2, f->Z[l - 1], B, L, f->dZc, f->dZt, f->grad + off_b(l - 1));
+        } else {
+            k_combine_bwd<<<cg, 256, 0, st>>>(f->Y1, f->Y2, nullptr, B, L, nullptr, nullptr, nullptr);
+            k_lift_wgrad<<<dim3(W, 8), 256, 0, st>>>(f->Y1, x, B, L, f->grad + OFF_P, f->grad + OFF_PB);
+        }
+    }
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+void fno_free(optifax_fno_s* f) {
+    void* ps[] = {f->master, f->grad, f->m, f->v, f->wb, f->wpt, f->F, f->FT, f->G, f->GT, f->T, f->dS, f->dZc,
+                  f->dZt, f->Y1, f->Y2, f->y, f->dy, f->dT, f->loss};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    for (int l = 0; l <= NLAYER; ++l) {
+        if (f->Hc[l]) cudaFree(f->Hc[l]);
+        if (f->Ht[l]) cudaFree(f->Ht[l]);
+    }
+    for (int l = 0; l < NLAYER; ++l)
+        if (f->S[l]) cudaFree(f->S[l]);
+    for (int l = 0; l < NLAYER - 1; ++l)
+        if (f->Z[l]) cudaFree(f->Z[l]);
+    delete f;
+}
+
+}  // namespace
+
+extern "C" int64_t optifax_fno_param_count(void) { return N_PARAMS; }
+
+extern "C" int optifax_fno_create(optifax_fno* out, int32_t n_bins, int32_t max_batch, int32_t device) {
+    if (!out) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (n_bins < 128 || n_bins % 64 || n_bins > (1 << 20) || max_batch < 1 || max_batch > 4096)
+        return OPTIFAX_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(device) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    optifax_fno_s* f = new optifax_fno_s();
+    f->device = device;
+    f->L = n_bins;
+    f->maxB = max_batch;
+    const long long L = n_bins, WB = (long long)W * max_batch, rowsA = WB > 128 ? WB : 128, BL = max_batch * L;
+    int rc = OPTIFAX_OK;
+    auto A = [&](auto** p, size_t bytes) {
+        if (!rc) rc = alloc0(p, bytes);
+    };
+    A(&f->master, sizeof(float) * N_PARAMS);
+    A(&f->grad, sizeof(float) * N_PARAMS);
+    A(&f->m, sizeof(float) * N_PARAMS);
+    A(&f->v, sizeof(float) * N_PARAMS);
+    A(&f->wb, sizeof(bf16) * N_PARAMS);
+    A(&f->wpt, sizeof(bf16) * NLAYER * W * W);
+    A(&f->F, sizeof(bf16) * SPEC * L);
+    A(&f->FT, sizeof(bf16) * SPEC * L);
+    A(&f->G, sizeof(bf16) * SPEC * L);
+    A(&f->GT, sizeof(bf16) * SPEC * L);
+    for (int l = 0; l <= NLAYER; ++l) {
+        A(&f->Hc[l], sizeof(bf16) * rowsA * L);
+        A(&f->Ht[l], sizeof(bf16) * BL * W);
+    }
+    for (int l = 0; l < NLAYER - 1; ++l) A(&f->Z[l], sizeof(float) * WB * L);
+    for (int l = 0; l < NLAYER; ++l) A(&f->S[l], sizeof(float) * WB * SPEC);
+    A(&f->T, sizeof(bf16) * rowsA * SPEC);
+    A(&f->dS, sizeof(bf16) * rowsA * SPEC);
+    A(&f->dZc, sizeof(bf16) * 2 * WB * L);     // the [o][(b,x)] view is read as 128 rows
+    A(&f->dZt, sizeof(bf16) * BL * W);
+    A(&f->Y1, sizeof(float) * WB * L);
+    A(&f->Y2, sizeof(float) * BL * W);
+    A(&f->y, sizeof(float) * BL * COUT);
+    A(&f->dy, sizeof(float) * BL * COUT);
+    A(&f->dT, sizeof(float) * WB * SPEC);
+    A(&f->loss, sizeof(float));
+    if (!rc) {
+        k_dft_tables<<<nblk((long long)SPEC * L), 256>>>((int)L, f->F, f->FT, f->G, f->GT);
+        if (cudaDeviceSynchronize() != cudaSuccess) rc = OPTIFAX_ERR_CUDA;
+    }
+    if (rc) {
+        fno_free(f);
+        return rc;
+    }
+    *out = f;
+    return OPTIFAX_OK;
+}
+
+extern "C" int optifax_fno_destroy(optifax_fno f) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    cudaSetDevice(f->device);
+    cudaDeviceSynchronize();
+    fno_free(f);
+    return OPTIFAX_OK;
+}
+
+extern "C" int optifax_fno_set_params(optifax_fno f, const float* params, void* stream) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!params) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemcpyAsync(f->master, params, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(f->m, 0, sizeof(float) * N_PARAMS, st) != cudaSuccess ||
+        cudaMemsetAsync(f->v, 0, sizeof(float) * N_PARAMS, st) != cudaSuccess)
+        return OPTIFAX_ERR_CUDA;
+    k_refresh<<<nblk(N_PARAMS), 256, 0, st>>>(f->master, f->wb, f->wpt);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+extern "C" int optifax_fno_get_params(optifax_fno f, float* params, void* stream) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!params) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    return cudaMemcpyAsync(params, f->master, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToDevice,
+                           static_cast<cudaStream_t>(stream)) == cudaSuccess
+               ? OPTIFAX_OK
+               : OPTIFAX_ERR_CUDA;
+}
+
+extern "C" int optifax_fno_forward(optifax_fno f, const float* x, float* y, int32_t batch, void* stream) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!x || batch < 1 || batch > f->maxB) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    OFX_TRY(fno_forward(f, x, batch, st));
+    if (y && cudaMemcpyAsync(y, f->y, sizeof(float) * (size_t)batch * COUT * f->L, cudaMemcpyDeviceToDevice, st) !=
+                 cudaSuccess)
+        return OPTIFAX_ERR_CUDA;
+    return OPTIFAX_OK;
+}
+
+extern "C" int optifax_fno_backward(optifax_fno f, const float* x, const float* target, int32_t batch, float* loss,
+                                    float* grads, void* stream) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!x || !target || batch < 1 || batch > f->maxB) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    OFX_TRY(fno_forward(f, x, batch, st));
+    OFX_TRY(fno_backward(f, x, target, batch, st));
+    if (loss && cudaMemcpyAsync(loss, f->loss, sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return OPTIFAX_ERR_CUDA;
+    if (grads && cudaMemcpyAsync(grads, f->grad, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+        return OPTIFAX_ERR_CUDA;
+    return OPTIFAX_OK;
+}
+
+extern "C" int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta2, float eps, float weight_decay,
+                                int32_t step, void* stream) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    if (step < 1 || !(lr >= 0.f)) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
+    k_adam<<<nblk(N_PARAMS), 256, 0, st>>>(f->master, f->grad, f->m, f->v, N_PARAMS, lr, beta1, beta2, eps,
+                                           weight_decay, bc1, bc2);
+    k_refresh<<<nblk(N_PARAMS), 256, 0, st>>>(f->master, f->wb, f->wpt);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}

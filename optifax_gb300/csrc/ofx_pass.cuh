@@ -61,6 +61,7 @@ struct PulseDev {
     optifax_trip_record* trips;
     int n_trips, n_tally, steady_trips, steady_tally;
     float steady_tol;
+    float2* hist;            // optional per-trip crystal-output spectra (n_trips x N)
     // cluster (C > 1) exchange scratch in global memory: 2 N complex
     float2* xch;
 };
@@ -669,6 +670,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
 #pragma unroll
                             for (int i = 0; i < 4; ++i)
                                 if (i < P.n_tally) part[i] = fmaf(P.tally_w[(size_t)i * N + kk], x2, part[i]);
+                            if (P.hist) P.hist[(size_t)trip * N + kk] = X;
                             v[j] = cadd(cmul(X, P.fb[kk]), P.pump[kk]);
                         } else {
                             v[j] = cmul(eh, dm1);

@@ -34,7 +34,7 @@ class OptifaxOpo(ctypes.Structure):
                 ("tally_w", ctypes.c_void_p), ("trips", ctypes.c_void_p),
                 ("n_trips", ctypes.c_int32), ("n_tally", ctypes.c_int32),
                 ("steady_trips", ctypes.c_int32), ("steady_tally", ctypes.c_int32),
-                ("steady_tol", ctypes.c_float), ("reserved", ctypes.c_int32)]
+                ("steady_tol", ctypes.c_float), ("reserved", ctypes.c_int32), ("history", ctypes.c_void_p)]
 
 
 TRIP_RECORD_BYTES = 48
@@ -113,6 +113,7 @@ class OpoResult:
     stats: dict
     trips_dev: Optional[torch.Tensor] = None
     stats_dev: Optional[torch.Tensor] = None
+    history: Optional[torch.Tensor] = None   # (n_trips, N) crystal-output spectra when requested
 
     def decode(self):
         """Copy the device records to the host (after the stream has finished)."""
@@ -151,7 +152,10 @@ class OpticalSim:
         self.trip_number = 0
 
     def run(self, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
-            steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True) -> OpoResult:
+            steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
+            history: bool = False) -> OpoResult:
+        """Run n_trips round trips in one launch.  history=True also returns every
+        trip's crystal-output spectrum X (n_trips, N) in ``result.history``."""
         si = self.arrays.si
         N = self.field.numel()
         out = torch.empty_like(self.field)
@@ -168,6 +172,8 @@ class OpticalSim:
         cv.trips = trips.data_ptr()
         cv.n_trips, cv.n_tally = int(n_trips), 4
         cv.steady_trips, cv.steady_tally, cv.steady_tol = int(steady_trips), int(steady_tally), float(steady_tol)
+        hist = torch.zeros((n_trips, N), dtype=torch.complex64, device=self.dev) if history else None
+        cv.history = hist.data_ptr() if hist is not None else None
         lib = self.ctx.lib
         lib.optifax_opo_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(OptifaxOpo), ctypes.c_int32,
                                         ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
@@ -176,6 +182,7 @@ class OpticalSim:
         nat.check(rc, self.ctx.handle, "optifax_opo_run")
         self.field = out
         res = OpoResult(field=out, trips=None, trips_done=-1, stats={}, trips_dev=trips, stats_dev=stats)
+        res.history = hist
         if not host_out:
             return res
         res.trips, res.trips_done, res.stats = res.decode()

@@ -14,7 +14,7 @@ def declared_functions():
         if fn.endswith(".h"):
             src = open(os.path.join(ROOT, "include", fn)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            names += re.findall(r"^\s*(?:int|const char\s*\*)\s+(optifax_\w+)\s*\(", src, flags=re.M)
+            names += re.findall(r"^\s*(?:int|int64_t|const char\s*\*)\s+(optifax_\w+)\s*\(", src, flags=re.M)
     return names
 
 
