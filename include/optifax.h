@@ -252,13 +252,13 @@ int optifax_tc_error(int32_t* out, int32_t clear);
 
 /*
  * Fourier-neural-operator surrogate of one crystal pass (no reference
- * counterpart).  Fixed architecture: 5 input channels (4 field channels + 1
- * constant conditioning channel) over n_bins frequency bins, width 64, four
- * spectral layers keeping 32 modes, GELU between layers, 4 output channels with a
+ * counterpart).  Fixed architecture: 6 input channels (4 field channels, a
+ * constant conditioning channel and the bin coordinate) over n_bins frequency
+ * bins, width 64, four spectral layers keeping 32 modes, GELU between layers, 4 output channels with a
  * residual connection to the first 4 inputs.  Parameters are one FP32 vector of
  * optifax_fno_param_count() values (layout in ofx_fno.cu); the kernels use BF16
  * copies of the weights and BF16 activations with FP32 accumulation.
- * x: DEVICE float [batch][5][n_bins]; y, target: DEVICE float [batch][4][n_bins].
+ * x: DEVICE float [batch][6][n_bins]; y, target: DEVICE float [batch][4][n_bins].
  * n_bins: a multiple of 64, >= 128.  One handle is used by one stream at a time.
  */
 typedef struct optifax_fno_s* optifax_fno;
@@ -269,13 +269,39 @@ int optifax_fno_destroy(optifax_fno f);
 int optifax_fno_set_params(optifax_fno f, const float* params, void* stream);
 int optifax_fno_get_params(optifax_fno f, float* params, void* stream);
 int optifax_fno_forward(optifax_fno f, const float* x, float* y, int32_t batch, void* stream);
-/* forward + backward of loss = mean((y - target)^2); loss (DEVICE scalar) and grads
+/* forward + backward of loss = sum_b w_b sum ((y - target)^2) / numel(y) with per-sample
+ * weights w (DEVICE, batch floats; NULL: all 1); loss (DEVICE scalar) and grads
  * (DEVICE, param_count floats) are optional copies of the results */
-int optifax_fno_backward(optifax_fno f, const float* x, const float* target, int32_t batch,
-                         float* loss, float* grads, void* stream);
+int optifax_fno_backward(optifax_fno f, const float* x, const float* target, const float* sample_w,
+                         int32_t batch, float* loss, float* grads, void* stream);
 /* AdamW step (decoupled weight decay) with the gradients of the last backward; step >= 1 */
 int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta2, float eps,
                      float weight_decay, int32_t step, void* stream);
+
+/*
+ * OPO fast-forward helpers (no reference counterpart).  A crop is n_bins
+ * consecutive bins of an n_points spectrum (natural FFT order of the fftshifted
+ * field, DEVICE complex64) starting at bin k0 and wrapping at n_points; crop bins
+ * j < split are the signal band.
+ * optifax_ff_encode: n_spectra spectra (stride elements apart) -> network input
+ * x[n][n_channels][n_bins]: channels 0/1 the pump band / pump_scale, 2/3 the signal
+ * band / sigma, 4 and 5 (if n_channels = 6) log10(sigma / pump_scale) and the bin
+ * coordinate j / n_bins.  sigma is the RMS of the signal-band bins (written to
+ * sigma_out) unless sigma_in supplies it.
+ * optifax_ff_step: X = the decoded network output y[4][n_bins] (with sigma[0]) times
+ * lin[k] (optional per-bin factor: the crystal's linear propagation, when the network
+ * predicts the output in the interaction picture), or X_in when y is NULL; writes
+ * X_out (optional), Y_next = X feedback + pump and (optional) *energy = sum tally_w |X|^2
+ * in FP64.  All pointers are device pointers.
+ */
+int optifax_ff_encode(const void* spectra, int64_t stride, int32_t n_spectra, int32_t n_points,
+                      int32_t k0, int32_t n_bins, int32_t split, float pump_scale,
+                      const float* sigma_in, float* x, int32_t n_channels, float* sigma_out,
+                      void* stream);
+int optifax_ff_step(const float* y, const float* sigma, const void* X_in, const void* feedback,
+                    const void* pump, const void* lin, const float* tally_w, int32_t n_points,
+                    int32_t k0, int32_t n_bins, int32_t split, float pump_scale, void* X_out,
+                    void* Y_next, double* energy, void* stream);
 
 #ifdef __cplusplus
 }

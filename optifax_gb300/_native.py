@@ -18,7 +18,8 @@ EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifa
            "optifax_opo_mex_batch", "optifax_propagate", "optifax_opo_run", "optifax_propagate_noalloc",
            "optifax_propagate_fp64", "optifax_gemm_bf16", "optifax_tc_error",
            "optifax_fno_param_count", "optifax_fno_create", "optifax_fno_destroy", "optifax_fno_set_params",
-           "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam"]
+           "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
+           "optifax_ff_encode", "optifax_ff_step"]
 
 _lib = None
 
@@ -98,10 +99,14 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_fno_get_params.restype = ctypes.c_int
     lib.optifax_fno_forward.argtypes = [vp, vp, vp, i32, vp]
     lib.optifax_fno_forward.restype = ctypes.c_int
-    lib.optifax_fno_backward.argtypes = [vp, vp, vp, i32, vp, vp, vp]
+    lib.optifax_fno_backward.argtypes = [vp, vp, vp, vp, i32, vp, vp, vp]
     lib.optifax_fno_backward.restype = ctypes.c_int
     lib.optifax_fno_adam.argtypes = [vp, f32, f32, f32, f32, f32, i32, vp]
     lib.optifax_fno_adam.restype = ctypes.c_int
+    lib.optifax_ff_encode.argtypes = [vp, i64, i32, i32, i32, i32, i32, f32, vp, vp, i32, vp, vp]
+    lib.optifax_ff_encode.restype = ctypes.c_int
+    lib.optifax_ff_step.argtypes = [vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, f32, vp, vp, vp, vp]
+    lib.optifax_ff_step.restype = ctypes.c_int
     _lib = lib
     return lib
 

@@ -2,8 +2,9 @@
 // backward and AdamW on the GPU.  No reference counterpart (the reference has no
 // learned component).
 //
-// Network (fixed sizes): input x[b][5][L] (4 field channels and one constant
-// conditioning channel over L frequency bins), lifting to width 64, four Fourier
+// Network (fixed sizes): input x[b][6][L] (4 field channels, one constant
+// conditioning channel and the bin coordinate over L frequency bins), lifting to
+// width 64, four Fourier
 // layers h <- act(SpecConv(h) + Wp h + bias) with 32 retained modes (no activation
 // after the last), projection to 4 channels plus a residual connection to the
 // first 4 input channels: y = x[:4] + Q h + q.
@@ -34,7 +35,7 @@ typedef __nv_bfloat16 bf16;
 
 namespace {
 
-constexpr int W = 64, MODES = 32, NLAYER = 4, CIN = 5, COUT = 4, SPEC = 2 * MODES;
+constexpr int W = 64, MODES = 32, NLAYER = 4, CIN = 6, COUT = 4, SPEC = 2 * MODES;
 constexpr long long LAYER_WS = (long long)W * W * MODES * 2;   // [c][o][m][re,im]
 constexpr long long LAYER_SIZE = LAYER_WS + W * W + W;         // Ws, Wp [o][c], bias [o]
 constexpr long long OFF_P = 0;                                 // [W][CIN]
@@ -198,14 +199,17 @@ __global__ void k_proj_fwd(const bf16* __restrict__ Ht, const bf16* __restrict__
 }
 
 // ---- loss and backward ---------------------------------------------------
-__global__ void k_loss(const float* __restrict__ y, const float* __restrict__ t, long long n, float inv_n,
-                       float* __restrict__ dy, float* __restrict__ loss) {
+// loss = sum_i w_(sample of i) (y_i - t_i)^2 / n  (w = 1 without sample weights)
+__global__ void k_loss(const float* __restrict__ y, const float* __restrict__ t, const float* __restrict__ w,
+                       long long per_sample, long long n, float inv_n, float* __restrict__ dy,
+                       float* __restrict__ loss) {
     __shared__ float red[32];
     float part = 0.f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float d = y[i] - t[i];
-        dy[i] = 2.f * d * inv_n;
-        part = fmaf(d, d, part);
+        const float wi = w ? w[i / per_sample] : 1.f;
+        dy[i] = 2.f * d * inv_n * wi;
+        part = fmaf(wi * d, d, part);
     }
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = part;
@@ -423,6 +427,100 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
     p[i] -= lr * ((mi / bc1) / (sqrtf(vi / bc2) + eps) + wd * p[i]);
 }
 
+// ---- OPO fast-forward: spectra <-> network channels ------------------------
+// The crop is n_bins consecutive bins of an N-point spectrum (natural FFT order)
+// starting at bin k0 (wrapping at N); bins j < split form the signal band.
+__global__ void k_ff_encode(const float2* __restrict__ Y, long long ystride, int N, int k0, int L, int split,
+                            float pump_scale, const float* __restrict__ sigma_in, float* __restrict__ x, int nch,
+                            float* __restrict__ sigma_out) {
+    __shared__ float red[32];
+    __shared__ float s_sigma;
+    const int p = blockIdx.x;
+    const float2* y = Y + p * ystride;
+    if (sigma_in) {
+        if (threadIdx.x == 0) s_sigma = sigma_in[p];
+    } else {
+        float acc = 0.f;
+        for (int j = threadIdx.x; j < split; j += blockDim.x) {
+            const float2 v = y[(k0 + j) % N];
+            acc = fmaf(v.x, v.x, fmaf(v.y, v.y, acc));
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float tot = 0.f;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+            float sg = sqrtf(tot / (float)(split > 0 ? split : 1));
+            const float floor_ = 1e-30f * pump_scale;
+            if (!(sg > floor_)) sg = floor_;
+            s_sigma = sg;
+            if (sigma_out) sigma_out[p] = sg;
+        }
+    }
+    __syncthreads();
+    const float sg = s_sigma, inv_s = 1.f / sg, inv_p = 1.f / pump_scale;
+    const float lg = log10f(sg * inv_p);
+    float* xo = x + (long long)p * nch * L;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        const float2 v = y[(k0 + j) % N];
+        const bool sb = j < split;
+        xo[j] = sb ? 0.f : v.x * inv_p;
+        xo[L + j] = sb ? 0.f : v.y * inv_p;
+        xo[2 * L + j] = sb ? v.x * inv_s : 0.f;
+        xo[3 * L + j] = sb ? v.y * inv_s : 0.f;
+        if (nch > 4) {
+            xo[4 * L + j] = lg;
+            xo[5 * L + j] = (float)j / (float)L;
+        }
+    }
+}
+
+// X = decoded network output times lin (or X_in); Y_next = X fb + pump; energy += sum tally_w |X|^2
+__global__ void k_ff_step(const float* __restrict__ y, const float* __restrict__ sigma, const float2* __restrict__ X_in,
+                          const float2* __restrict__ fb, const float2* __restrict__ pump,
+                          const float2* __restrict__ lin, const float* __restrict__ tw, int N, int k0, int L,
+                          int split, float pump_scale, float2* __restrict__ X_out, float2* __restrict__ Y_next,
+                          double* __restrict__ energy) {
+    __shared__ double red[32];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    if (k < N) {
+        float2 X = make_float2(0.f, 0.f);
+        if (y) {
+            const int j = (k - k0 + N) % N;
+            if (j < L) {
+                if (j < split) {
+                    const float sg = sigma[0];
+                    X = make_float2(y[2 * L + j] * sg, y[3 * L + j] * sg);
+                } else {
+                    X = make_float2(y[j] * pump_scale, y[L + j] * pump_scale);
+                }
+                if (lin) {
+                    const float2 d = lin[k];
+                    X = make_float2(X.x * d.x - X.y * d.y, X.x * d.y + X.y * d.x);
+                }
+            }
+        } else {
+            X = X_in[k];
+        }
+        if (X_out) X_out[k] = X;
+        const float2 f = fb[k], pp = pump[k];
+        Y_next[k] = make_float2(X.x * f.x - X.y * f.y + pp.x, X.x * f.y + X.y * f.x + pp.y);
+        if (tw) e = (double)tw[k] * ((double)X.x * X.x + (double)X.y * X.y);
+    }
+    if (energy) {
+        for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+            atomicAdd(energy, tot);
+        }
+    }
+}
+
 inline unsigned nblk(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
@@ -473,14 +571,15 @@ int fno_forward(optifax_fno_s* f, const float* x, int B, cudaStream_t st) {
     return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
 }
 
-int fno_backward(optifax_fno_s* f, const float* x, const float* target, int B, cudaStream_t st) {
+int fno_backward(optifax_fno_s* f, const float* x, const float* target, const float* sample_w, int B,
+                 cudaStream_t st) {
     const int L = f->L;
     const long long WB = (long long)W * B, rowsA = WB > 128 ? WB : 128, BL = (long long)B * L;
     if (cudaMemsetAsync(f->grad, 0, sizeof(float) * N_PARAMS, st) != cudaSuccess ||
         cudaMemsetAsync(f->loss, 0, sizeof(float), st) != cudaSuccess)
         return OPTIFAX_ERR_CUDA;
     const long long ny = BL * COUT;
-    k_loss<<<256, 256, 0, st>>>(f->y, target, ny, 1.f / (float)ny, f->dy, f->loss);
+    k_loss<<<256, 256, 0, st>>>(f->y, target, sample_w, (long long)COUT * L, ny, 1.f / (float)ny, f->dy, f->loss);
     k_proj_bwd<<<nblk(BL), 256, 0, st>>>(f->dy, f->wb + OFF_Q, B, L, f->dZc, f->dZt, f->grad + off_b(NLAYER - 1));
     const int rpb = 2048;
     k_proj_wgrad<<<nblk(BL, rpb), 256, 0, st>>>(f->dy, f->Ht[NLAYER], B, L, rpb, f->grad + OFF_Q, f->grad + OFF_QB);
@@ -618,13 +717,13 @@ extern "C" int optifax_fno_forward(optifax_fno f, const float* x, float* y, int3
     return OPTIFAX_OK;
 }
 
-extern "C" int optifax_fno_backward(optifax_fno f, const float* x, const float* target, int32_t batch, float* loss,
-                                    float* grads, void* stream) {
+extern "C" int optifax_fno_backward(optifax_fno f, const float* x, const float* target, const float* sample_w,
+                                    int32_t batch, float* loss, float* grads, void* stream) {
     if (!f) return OPTIFAX_ERR_NULL_HANDLE;
     if (!x || !target || batch < 1 || batch > f->maxB) return OPTIFAX_ERR_INVALID_ARGUMENT;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     OFX_TRY(fno_forward(f, x, batch, st));
-    OFX_TRY(fno_backward(f, x, target, batch, st));
+    OFX_TRY(fno_backward(f, x, target, sample_w, batch, st));
     if (loss && cudaMemcpyAsync(loss, f->loss, sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
         return OPTIFAX_ERR_CUDA;
     if (grads && cudaMemcpyAsync(grads, f->grad, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
@@ -641,5 +740,35 @@ extern "C" int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta
     k_adam<<<nblk(N_PARAMS), 256, 0, st>>>(f->master, f->grad, f->m, f->v, N_PARAMS, lr, beta1, beta2, eps,
                                            weight_decay, bc1, bc2);
     k_refresh<<<nblk(N_PARAMS), 256, 0, st>>>(f->master, f->wb, f->wpt);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+extern "C" int optifax_ff_encode(const void* spectra, int64_t stride, int32_t n_spectra, int32_t n_points, int32_t k0,
+                                 int32_t n_bins, int32_t split, float pump_scale, const float* sigma_in, float* x,
+                                 int32_t n_channels, float* sigma_out, void* stream) {
+    if (!spectra || !x || n_spectra < 1 || n_points < 1 || n_bins < 1 || n_bins > n_points || k0 < 0 ||
+        k0 >= n_points || split < 0 || split > n_bins || stride < n_points || !(pump_scale > 0.f) ||
+        (n_channels != 4 && n_channels != 6))
+        return OPTIFAX_ERR_INVALID_ARGUMENT;
+    k_ff_encode<<<n_spectra, 1024, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float2*>(spectra), stride, n_points, k0, n_bins, split, pump_scale, sigma_in, x, n_channels,
+        sigma_out);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+extern "C" int optifax_ff_step(const float* y, const float* sigma, const void* X_in, const void* feedback,
+                               const void* pump, const void* lin, const float* tally_w, int32_t n_points, int32_t k0,
+                               int32_t n_bins, int32_t split, float pump_scale, void* X_out, void* Y_next,
+                               double* energy, void* stream) {
+    if ((!y && !X_in) || (y && !sigma) || !feedback || !pump || !Y_next || n_points < 1 || n_bins < 1 ||
+        n_bins > n_points || k0 < 0 || k0 >= n_points || split < 0 || split > n_bins || !(pump_scale > 0.f))
+        return OPTIFAX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (energy && cudaMemsetAsync(energy, 0, sizeof(double), st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    k_ff_step<<<nblk(n_points), 256, 0, st>>>(y, sigma, static_cast<const float2*>(X_in),
+                                              static_cast<const float2*>(feedback), static_cast<const float2*>(pump),
+                                              static_cast<const float2*>(lin), tally_w, n_points, k0, n_bins, split,
+                                              pump_scale, static_cast<float2*>(X_out), static_cast<float2*>(Y_next),
+                                              energy);
     return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
 }

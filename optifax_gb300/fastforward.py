@@ -1,0 +1,351 @@
+"""Surrogate fast-forward of synchronously pumped OPO round trips.
+
+A trained FNO (optifax_gb300.surrogate) replaces the crystal pass for most
+round trips; the solver checks it every ``check_every`` trips, takes over
+whenever the check fails, and finishes every run (with its own steady-state
+test).  No reference counterpart: the reference runs every trip through its
+solver (OpticalSim.m:230-288).
+
+Frequency crop (``Crop``): n_bins consecutive bins of the 2^14-point spectrum
+starting at F_LO = 140 THz (the signal band 166-222 THz and the 288 THz pump fit
+inside); bins below F_SPLIT = 250 THz are the signal band, the rest the pump
+band.  Everything outside the crop is dropped: the cavity feeds back only the
+signal band and the pump is injected fresh every trip.
+
+Interaction picture: the network predicts the crystal output divided by the
+crystal's linear propagation D_k = alpha_k^S exp(-i beta_k S) (known exactly),
+so it learns only the nonlinear change, not the large dispersion phase.
+
+Training pairs come from the solver itself: cavities of the 2^14-point, 5 mm
+SPOPO geometry with pump power and width drawn from the sweep ranges (0.5-3 W,
+100-300 fs, seeded), each run for n_trips round trips in one launch with the
+per-trip crystal-output spectra recorded; pair t is (crystal input Y_t, crystal
+output X_t) with Y_0 = FFT(E_0) and Y_{t+1} = X_t feedback + pump.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import time
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from . import opo
+from .surrogate import FNO, COUT, CIN
+
+F_LO = 140e12
+F_SPLIT = 250e12
+N_BINS = 4096
+
+
+@dataclasses.dataclass
+class Crop:
+    n_points: int
+    k0: int
+    n_bins: int
+    split: int
+    pump_scale: float
+
+
+def make_crop(win, pump_scale: float, n_bins: int = N_BINS, f_lo: float = F_LO, f_split: float = F_SPLIT) -> Crop:
+    n = win.n_points
+    df = 1.0 / (n * win.dt)
+    f0 = win.f0
+    k_lo = int(round((f_lo - f0) / df))
+    split = int(math.ceil((f_split - (f0 + k_lo * df)) / df))
+    if not (0 < split < n_bins <= n):
+        raise ValueError("crop does not hold both bands")
+    return Crop(n, k_lo % n, n_bins, split, float(pump_scale))
+
+
+def reference_crop(spec: Optional[opo.CavitySpec] = None) -> Crop:
+    """Crop with the pump scale of the 2 W, 200 fs pump of the given geometry."""
+    spec = spec or opo.CavitySpec()
+    ref = dataclasses.replace(spec, pump_power=2.0, pump_tau=200e-15)
+    a = opo.build_cavity(ref)
+    return make_crop(a.win, float(np.max(np.abs(a.pump))))
+
+
+def _ptr(t):
+    return t.data_ptr() if t is not None else None
+
+
+def _stream(dev):
+    return int(torch.cuda.current_stream(dev).cuda_stream)
+
+
+def encode(spectra: torch.Tensor, crop: Crop, sigma_in: Optional[torch.Tensor] = None, n_channels: int = CIN):
+    """(P, N) complex64 spectra -> (x (P, n_channels, n_bins) float32, sigma (P,))."""
+    spectra = spectra.contiguous()
+    P = spectra.shape[0]
+    dev = spectra.device
+    x = torch.empty((P, n_channels, crop.n_bins), dtype=torch.float32, device=dev)
+    sig = sigma_in.contiguous() if sigma_in is not None else torch.empty(P, dtype=torch.float32, device=dev)
+    rc = nat.load().optifax_ff_encode(spectra.data_ptr(), spectra.stride(0), P, crop.n_points, crop.k0,
+                                      crop.n_bins, crop.split, crop.pump_scale,
+                                      _ptr(sigma_in), x.data_ptr(), n_channels,
+                                      None if sigma_in is not None else sig.data_ptr(), _stream(dev))
+    nat.check(rc, None, "optifax_ff_encode")
+    return x, sig
+
+
+def step(crop: Crop, feedback, pump, tally_w, *, y=None, sigma=None, lin=None, X_in=None, X_out=None,
+         Y_next=None, energy=None):
+    """X from the network output y (decoded with sigma, times lin) or X_in; returns
+    Y_next = X fb + pump (and fills energy = sum tally_w |X|^2 when given)."""
+    dev = feedback.device
+    if Y_next is None:
+        Y_next = torch.empty(crop.n_points, dtype=torch.complex64, device=dev)
+    rc = nat.load().optifax_ff_step(_ptr(y), _ptr(sigma), _ptr(X_in), feedback.data_ptr(), pump.data_ptr(),
+                                    _ptr(lin), _ptr(tally_w), crop.n_points, crop.k0, crop.n_bins, crop.split,
+                                    crop.pump_scale, _ptr(X_out), Y_next.data_ptr(), _ptr(energy), _stream(dev))
+    nat.check(rc, None, "optifax_ff_step")
+    return Y_next
+
+
+def linear_factor(sim: opo.OpticalSim) -> torch.Tensor:
+    """The crystal's linear propagation per bin, D_k = alpha_k^S exp(-i beta_k S) (the
+    dispersion sub-steps of a whole pass, natural FFT order)."""
+    si = sim.arrays.si
+    S = si.n_steps
+    a = np.asarray(si.alpha, dtype=np.float64) ** S
+    D = a * np.exp(-1j * np.asarray(si.beta, dtype=np.float64) * S)
+    return torch.from_numpy(D.astype(np.complex64)).to(sim.dev)
+
+
+def to_interaction(X: torch.Tensor, D: torch.Tensor) -> torch.Tensor:
+    """X / D where |D| > 0, else 0."""
+    m = D.abs() > 0
+    den = torch.where(m, D.abs() ** 2, torch.ones_like(D.real))
+    return torch.where(m, X * torch.conj(D) / den, torch.zeros_like(X))
+
+
+# --------------------------------------------------------------------------
+# Training data from the solver
+# --------------------------------------------------------------------------
+def training_specs(n: int, seed: int = 3, power=(0.5, 3.0), tau=(100e-15, 300e-15),
+                   base: Optional[opo.CavitySpec] = None) -> List[opo.CavitySpec]:
+    rng = np.random.default_rng(seed)
+    base = base or opo.CavitySpec()
+    return [dataclasses.replace(base, pump_power=float(rng.uniform(*power)), pump_tau=float(rng.uniform(*tau)),
+                                seed=seed * 100000 + i) for i in range(n)]
+
+
+def generate_pairs(specs: List[opo.CavitySpec], n_trips: int, crop: Crop, device: int = 0, group: int = 38):
+    """Run the cavities (group at a time, one launch per group) and return the
+    encoded pairs (x (P, 6, L), interaction-picture target (P, 4, L)), the trip
+    index of every pair and the solver attempt count."""
+    dev = torch.device(f"cuda:{device}")
+    xs, ts, trip_idx = [], [], []
+    attempts = 0
+    for g0 in range(0, len(specs), group):
+        sims = [opo.OpticalSim(s, device=device) for s in specs[g0:g0 + group]]
+        Y0 = [torch.from_numpy(np.fft.fft(s.arrays.E0).astype(np.complex64)).to(dev) for s in sims]
+        res = opo.run_many(sims, n_trips, history=True)
+        for sim, r, y0 in zip(sims, res, Y0):
+            attempts += int(np.sum(r.trips["attempts"]))
+            hist = r.history[:r.trips_done]
+            ins = torch.empty_like(hist)
+            ins[0] = y0
+            if hist.shape[0] > 1:
+                ins[1:] = hist[:-1] * sim.feedback + sim.pump
+            x, sig = encode(ins, crop)
+            t, _ = encode(to_interaction(hist, linear_factor(sim)), crop, sigma_in=sig, n_channels=COUT)
+            xs.append(x)
+            ts.append(t)
+            trip_idx.append(torch.arange(hist.shape[0]))
+        del sims, res
+    return torch.cat(xs), torch.cat(ts), torch.cat(trip_idx), attempts
+
+
+def signal_rel_err(y: torch.Tensor, t: torch.Tensor) -> torch.Tensor:
+    """Per-sample relative L2 error of the signal channels (2, 3)."""
+    d = (y[:, 2:4] - t[:, 2:4]).flatten(1).norm(dim=1)
+    return d / t[:, 2:4].flatten(1).norm(dim=1).clamp_min(1e-30)
+
+
+def sample_weights(T: torch.Tensor) -> torch.Tensor:
+    """Per-sample loss weights 1 / mean(target^2): every pair counts by its relative
+    error, so the large normalised gains of the build-up trips do not swamp the rest."""
+    return 1.0 / T.pow(2).mean(dim=(1, 2)).clamp_min(1e-12)
+
+
+def evaluate(net: FNO, X: torch.Tensor, T: torch.Tensor, batch: Optional[int] = None) -> torch.Tensor:
+    batch = batch or net.max_batch
+    errs = []
+    for i in range(0, X.shape[0], batch):
+        y = net.forward(X[i:i + batch].contiguous())
+        errs.append(signal_rel_err(y, T[i:i + batch]))
+    return torch.cat(errs)
+
+
+def train(net: FNO, X: torch.Tensor, T: torch.Tensor, *, epochs: int = 40, batch: int = 32, lr: float = 1e-3,
+          val_frac: float = 0.05, seed: int = 3, weight_decay: float = 0.0, trip_idx=None, log=None) -> dict:
+    """AdamW with cosine-decayed learning rate on shuffled minibatches, relative
+    (per-sample weighted) squared error; returns the history."""
+    P = X.shape[0]
+    g = torch.Generator().manual_seed(seed)
+    perm = torch.randperm(P, generator=g)
+    n_val = max(1, int(P * val_frac))
+    val, tr = perm[:n_val], perm[n_val:]
+    Wt = sample_weights(T)
+    steps_per_epoch = max(1, len(tr) // batch)
+    total = epochs * steps_per_epoch
+    hist = {"train_loss": [], "val_signal_rel_l2": [], "epochs": epochs, "pairs": P, "val_pairs": n_val}
+    step_i = 0
+    t0 = time.perf_counter()
+    vdev = val.to(X.device)
+    for ep in range(epochs):
+        order = tr[torch.randperm(len(tr), generator=g)]
+        acc = torch.zeros(1, device=net.dev)
+        for s_ in range(steps_per_epoch):
+            idx = order[s_ * batch:(s_ + 1) * batch].to(net.dev)
+            loss = net.backward(X.index_select(0, idx), T.index_select(0, idx), sample_w=Wt.index_select(0, idx))
+            acc += loss
+            cur = lr * 0.5 * (1.0 + math.cos(math.pi * step_i / total))
+            net.adam(cur, weight_decay=weight_decay)
+            step_i += 1
+        hist["train_loss"].append(float(acc.item()) / steps_per_epoch)
+        ve = evaluate(net, X[vdev], T[vdev])
+        hist["val_signal_rel_l2"].append(float(ve.median()))
+        if log:
+            log(f"epoch {ep}: train {hist['train_loss'][-1]:.4e} val signal rel-L2 median "
+                f"{hist['val_signal_rel_l2'][-1]:.4e}")
+    torch.cuda.synchronize(net.dev)
+    hist["seconds"] = time.perf_counter() - t0
+    hist["steps"] = step_i
+    ve = evaluate(net, X[vdev], T[vdev]).cpu()
+    hist["val_signal_rel_l2_quantiles"] = [float(v) for v in torch.quantile(ve, torch.tensor([0.1, 0.5, 0.9]))]
+    if trip_idx is not None:
+        ti = trip_idx[val]
+        bins = [(0, 20), (20, 60), (60, 10 ** 9)]
+        hist["val_by_trip"] = {f"{a}-{b}": float(ve[(ti >= a) & (ti < b)].median())
+                               for a, b in bins if bool(((ti >= a) & (ti < b)).any())}
+    return hist
+
+
+# --------------------------------------------------------------------------
+# The fast-forward OPO run
+# --------------------------------------------------------------------------
+def _to_time(Y: torch.Tensor) -> torch.Tensor:
+    """Crystal input field (fftshifted time) from its spectrum: the solver's E_in
+    (host FFT, once per hand-over to the solver)."""
+    e = np.fft.ifft(Y.cpu().numpy().astype(np.complex128))
+    return torch.from_numpy(e.astype(np.complex64)).to(Y.device)
+
+
+def _to_spec(E: torch.Tensor) -> torch.Tensor:
+    return torch.from_numpy(np.fft.fft(E.cpu().numpy().astype(np.complex128)).astype(np.complex64)).to(E.device)
+
+
+def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop: Crop, *, max_trips: int = 1000,
+                     check_every: int = 10, check_tol: float = 0.05, finish_trips: int = 50,
+                     flat_tol: float = 1e-3, steady_tol: float = 1e-4, steady_trips: int = 10) -> dict:
+    """max_trips round trips from sim's current state.
+
+    Blocks of check_every trips: the first trip of a block is the check (the
+    network's prediction and a solver pass from the same input; the cavity
+    continues from the solver's result); when the relative L2 difference over the
+    fed-back band is within check_tol the other trips of the block run on the
+    network, otherwise on the solver.  The last finish_trips trips (and everything
+    after the network's trips level out to flat_tol) run on the solver, which
+    stops early once its steady-state test passes.  net=None runs the solver only.
+    """
+    dev = sim.dev
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    tw_sig = sim.tally_w[opo.TALLY_OUTPUT_SIGNAL]
+    fbm = sim.feedback.abs() > 0
+    D = linear_factor(sim)
+    energy = torch.zeros(1, dtype=torch.float64, device=dev)
+    trips = sur_trips = sol_trips = 0
+    checks, energies = [], []
+    fallback_blocks = 0
+    Y = _to_spec(sim.field) if net is not None else None
+    surrogate_until = max_trips - finish_trips if net is not None else 0
+    while trips < surrogate_until:
+        # check trip
+        x, sig = encode(Y.unsqueeze(0), crop)
+        y = net.forward(x)
+        Xs = torch.empty(crop.n_points, dtype=torch.complex64, device=dev)
+        step(crop, sim.feedback, sim.pump, None, y=y, sigma=sig, lin=D, X_out=Xs)
+        sim.field = _to_time(Y)
+        r = sim.run(1, history=True)
+        Xt = r.history[0]
+        Y = step(crop, sim.feedback, sim.pump, tw_sig, X_in=Xt, energy=energy)
+        energies.append(float(energy.item()))
+        trips += 1
+        sol_trips += 1
+        err = float(((Xs - Xt)[fbm]).abs().norm() / Xt[fbm].abs().norm().clamp_min(1e-30))
+        checks.append(err)
+        n = min(check_every - 1, surrogate_until - trips)
+        if n <= 0:
+            break
+        if err <= check_tol:                         # NaN fails too
+            for _ in range(n):
+                x, sig = encode(Y.unsqueeze(0), crop)
+                y = net.forward(x)
+                Y = step(crop, sim.feedback, sim.pump, tw_sig, y=y, sigma=sig, lin=D, energy=energy)
+                energies.append(float(energy.item()))
+                trips += 1
+                sur_trips += 1
+            if not all(math.isfinite(e) for e in energies[-n:]):
+                break
+        else:
+            sim.field = _to_time(Y)
+            r = sim.run(n)
+            trips += r.trips_done
+            sol_trips += r.trips_done
+            energies += [float(v) for v in r.trips["tally"][:, opo.TALLY_OUTPUT_SIGNAL]]
+            Y = _to_spec(sim.field)
+            fallback_blocks += 1
+        if len(energies) > steady_trips:
+            e = np.array(energies[-(steady_trips + 1):])
+            if np.all(np.abs(np.diff(e)) <= flat_tol * np.abs(e[1:])):
+                break
+    finish = 0
+    if trips < max_trips:
+        if Y is not None:
+            sim.field = _to_time(Y)
+        r = sim.run(max_trips - trips, steady_tol=steady_tol, steady_trips=steady_trips)
+        finish = r.trips_done
+        trips += finish
+        sol_trips += finish
+        energies += [float(v) for v in r.trips["tally"][:, opo.TALLY_OUTPUT_SIGNAL]]
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    flat = len(energies) > steady_trips and bool(np.all(
+        np.abs(np.diff(energies[-(steady_trips + 1):])) <= steady_tol * np.abs(energies[-steady_trips:])))
+    return {"trips": trips, "surrogate_trips": sur_trips, "solver_trips": sol_trips, "finish_trips": finish,
+            "checks": checks, "fallback_blocks": fallback_blocks, "wall_s": wall,
+            "trips_per_s": trips / wall if wall > 0 else float("nan"),
+            "final_output_signal_energy": energies[-1] if energies else float("nan"),
+            "reached_steady_state": flat, "energies": energies, "field": sim.field}
+
+
+def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0=None) -> dict:
+    """Round trips through the plain FP64 solver (optifax_propagate_fp64) with the
+    cavity transfer in FP64 on the host; returns seconds per trip."""
+    from . import solver as sv
+    a = opo.build_cavity(spec)
+    si = a.si
+    dev = torch.device(f"cuda:{device}")
+    t64 = lambda v: torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
+    al, be, G = t64(si.alpha), t64(si.beta), t64(si.G)
+    E = np.asarray(a.E0 if E0 is None else E0, dtype=np.complex128)
+    attempts = 0
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(n_trips):
+        A, st, _ = sv.propagate_fp64(torch.from_numpy(E).to(dev), al, be, G, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                                     dt=si.dt, n_steps=si.n_steps, max_err=si.max_err, min_err=si.min_err,
+                                     sel=si.sel)
+        attempts += st["attempts"]
+        X = np.fft.fft(A.cpu().numpy())
+        E = np.fft.ifft(X * a.feedback + a.pump)
+    wall = time.perf_counter() - t0
+    return {"trips": n_trips, "wall_s": wall, "s_per_trip": wall / n_trips, "trips_per_s": n_trips / wall,
+            "attempts": attempts, "field": E}

@@ -151,16 +151,11 @@ class OpticalSim:
         self.ctx = context(device)
         self.trip_number = 0
 
-    def run(self, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
-            steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
-            history: bool = False) -> OpoResult:
-        """Run n_trips round trips in one launch.  history=True also returns every
-        trip's crystal-output spectrum X (n_trips, N) in ``result.history``."""
+    def _descriptor(self, n_trips, steady_tol, steady_trips, steady_tally, history):
         si = self.arrays.si
         N = self.field.numel()
         out = torch.empty_like(self.field)
         trips = torch.zeros((n_trips, TRIP_RECORD_BYTES // 4), dtype=torch.int32, device=self.dev)
-        stats = torch.zeros((1, nat.STATS_BYTES // 4), dtype=torch.int32, device=self.dev)
         cv = OptifaxOpo()
         d = cv.pass_
         d.n_points, d.n_steps = N, si.n_steps
@@ -174,17 +169,48 @@ class OpticalSim:
         cv.steady_trips, cv.steady_tally, cv.steady_tol = int(steady_trips), int(steady_tally), float(steady_tol)
         hist = torch.zeros((n_trips, N), dtype=torch.complex64, device=self.dev) if history else None
         cv.history = hist.data_ptr() if hist is not None else None
-        lib = self.ctx.lib
-        lib.optifax_opo_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(OptifaxOpo), ctypes.c_int32,
-                                        ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
-        rc = lib.optifax_opo_run(self.ctx.handle, ctypes.byref(cv), 1, int(self.variant),
-                                 int(self.cta_points), stats.data_ptr(), _stream_ptr(stream))
-        nat.check(rc, self.ctx.handle, "optifax_opo_run")
-        self.field = out
-        res = OpoResult(field=out, trips=None, trips_done=-1, stats={}, trips_dev=trips, stats_dev=stats)
+        return cv, out, trips, hist
+
+    def run(self, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
+            steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
+            history: bool = False) -> OpoResult:
+        """Run n_trips round trips in one launch.  history=True also returns every
+        trip's crystal-output spectrum X (n_trips, N) in ``result.history``."""
+        return run_many([self], n_trips, steady_tol=steady_tol, steady_trips=steady_trips,
+                        steady_tally=steady_tally, stream=stream, host_out=host_out, history=history)[0]
+
+
+def run_many(sims, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
+             steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
+             history: bool = False):
+    """Run several independent cavities (same device) for n_trips each in one launch."""
+    if not sims:
+        raise ValueError("no cavities")
+    dev = sims[0].dev
+    arr = (OptifaxOpo * len(sims))()
+    outs = []
+    for i, sim in enumerate(sims):
+        if sim.dev != dev or sim.variant != sims[0].variant:
+            raise ValueError("cavities of one launch share the device and the variant")
+        cv, out, trips, hist = sim._descriptor(n_trips, steady_tol, steady_trips, steady_tally, history)
+        arr[i] = cv
+        outs.append((out, trips, hist))
+    stats = torch.zeros((len(sims), nat.STATS_BYTES // 4), dtype=torch.int32, device=dev)
+    ctx = sims[0].ctx
+    lib = ctx.lib
+    lib.optifax_opo_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(OptifaxOpo), ctypes.c_int32,
+                                    ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    rc = lib.optifax_opo_run(ctx.handle, arr, len(sims), int(sims[0].variant), int(sims[0].cta_points),
+                             stats.data_ptr(), _stream_ptr(stream))
+    nat.check(rc, ctx.handle, "optifax_opo_run")
+    results = []
+    for i, (sim, (out, trips, hist)) in enumerate(zip(sims, outs)):
+        sim.field = out
+        res = OpoResult(field=out, trips=None, trips_done=-1, stats={}, trips_dev=trips,
+                        stats_dev=stats[i:i + 1])
         res.history = hist
-        if not host_out:
-            return res
-        res.trips, res.trips_done, res.stats = res.decode()
-        self.trip_number += res.trips_done
-        return res
+        if host_out:
+            res.trips, res.trips_done, res.stats = res.decode()
+            sim.trip_number += res.trips_done
+        results.append(res)
+    return results

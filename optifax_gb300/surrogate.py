@@ -11,7 +11,9 @@ Field encoding (``Encoder``): the crystal-input and crystal-output spectra of a
 pump band (frequencies at or above ``f_split``) scaled by the fixed pump scale,
 channels 2/3 the signal band (below ``f_split``) scaled by the input signal's own
 RMS ``sigma``; channel 4 is the constant log10(sigma / pump scale), so the
-network sees amplitude and shape separately (the small-signal map is linear).
+network sees amplitude and shape separately (the small-signal map is linear),
+and channel 5 the bin coordinate j / n_bins (the layers are otherwise
+translation-equivariant along the bins).
 The output uses the same scales, so an output decodes with the input's sigma.
 """
 from __future__ import annotations
@@ -26,7 +28,7 @@ import torch
 
 from . import _native as nat
 
-W, MODES, NLAYER, CIN, COUT = 64, 32, 4, 5, 4
+W, MODES, NLAYER, CIN, COUT = 64, 32, 4, 6, 4
 LAYER_WS = W * W * MODES * 2
 LAYER_SIZE = LAYER_WS + W * W + W
 OFF_P, OFF_PB = 0, W * CIN
@@ -95,11 +97,18 @@ class FNO:
                   None, "fno_forward")
         return y
 
-    def backward(self, x: torch.Tensor, target: torch.Tensor, grads: Optional[torch.Tensor] = None, stream=None):
-        """Forward + backward; returns the device loss tensor (1,) (grads copied if given)."""
+    def backward(self, x: torch.Tensor, target: torch.Tensor, grads: Optional[torch.Tensor] = None,
+                 sample_w: Optional[torch.Tensor] = None, stream=None):
+        """Forward + backward of sum_b w_b |y_b - t_b|^2 / numel; returns the device loss
+        tensor (1,) (grads copied if given)."""
         x = self._check_x(x, CIN)
         target = self._check_x(target, COUT)
-        nat.check(self.lib.optifax_fno_backward(self.h, x.data_ptr(), target.data_ptr(), x.shape[0],
+        if sample_w is not None:
+            sample_w = sample_w.to(torch.float32).contiguous()
+            if sample_w.numel() != x.shape[0] or sample_w.device != self.dev:
+                raise ValueError("sample_w must hold one weight per sample on the network's device")
+        nat.check(self.lib.optifax_fno_backward(self.h, x.data_ptr(), target.data_ptr(),
+                                                sample_w.data_ptr() if sample_w is not None else None, x.shape[0],
                                                 self.loss_dev.data_ptr(),
                                                 grads.data_ptr() if grads is not None else None, self._s(stream)),
                   None, "fno_backward")

@@ -20,7 +20,7 @@ import math
 
 import numpy as np
 
-W, MODES, NLAYER, CIN, COUT = 64, 32, 4, 5, 4
+W, MODES, NLAYER, CIN, COUT = 64, 32, 4, 6, 4
 LAYER_WS = W * W * MODES * 2
 LAYER_SIZE = LAYER_WS + W * W + W
 OFF_P = 0
@@ -92,7 +92,7 @@ def _ispec(T, L):
 
 
 def forward(params, x, weights_bf16=True):
-    """x (B, 5, L) -> (y (B, 4, L), cache)."""
+    """x (B, 6, L) -> (y (B, 4, L), cache)."""
     w = unpack(params, weights_bf16)
     x = np.asarray(x, dtype=np.float64)
     L = x.shape[-1]
@@ -110,14 +110,15 @@ def forward(params, x, weights_bf16=True):
     return y, cache
 
 
-def loss_and_grads(params, x, target, weights_bf16=True):
-    """(loss, flat gradient vector, y)."""
+def loss_and_grads(params, x, target, weights_bf16=True, sample_w=None):
+    """(loss, flat gradient vector, y); loss = sum_b w_b sum (y_b - t_b)^2 / y.size."""
     y, c = forward(params, x, weights_bf16)
     w = c["w"]
     t = np.asarray(target, dtype=np.float64)
     n = y.size
-    loss = float(np.sum((y - t) ** 2) / n)
-    dy = 2.0 * (y - t) / n
+    sw = np.ones(y.shape[0]) if sample_w is None else np.asarray(sample_w, dtype=np.float64)
+    loss = float(np.sum(sw[:, None, None] * (y - t) ** 2) / n)
+    dy = 2.0 * sw[:, None, None] * (y - t) / n
     g = {"Q": np.einsum("bjx,bcx->jc", dy, c["h"][NLAYER]), "q": dy.sum(axis=(0, 2)), "layers": [None] * NLAYER}
     dh = np.einsum("jc,bjx->bcx", w["Q"], dy)
     L = y.shape[-1]

@@ -1,0 +1,60 @@
+"""Fast-forward helpers and the surrogate/solver hand-over.  Marked gpu."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_encode_and_step_match_numpy():
+    from optifax_gb300 import fastforward as ff, physics as ph
+    win = ph.SimWindow(1040e-9, 2 ** 14, 12e-12)
+    crop = ff.make_crop(win, pump_scale=3.0)
+    rng = np.random.default_rng(0)
+    N, L, s = crop.n_points, crop.n_bins, crop.split
+    Y = (rng.normal(size=(2, N)) + 1j * rng.normal(size=(2, N))).astype(np.complex64)
+    dev = torch.device("cuda:0")
+    x, sig = ff.encode(torch.from_numpy(Y).to(dev), crop)
+    x, sig = x.cpu().numpy(), sig.cpu().numpy()
+    idx = (crop.k0 + np.arange(L)) % N
+    for p in range(2):
+        c = Y[p, idx].astype(np.complex128)
+        sg = np.sqrt(np.mean(np.abs(c[:s]) ** 2))
+        assert abs(sig[p] - sg) <= 1e-5 * sg
+        assert np.allclose(x[p, 2, :s] + 1j * x[p, 3, :s], c[:s] / sg, atol=1e-5)
+        assert np.allclose(x[p, 0, s:] + 1j * x[p, 1, s:], c[s:] / 3.0, atol=1e-5)
+        assert np.all(x[p, 0, :s] == 0) and np.all(x[p, 2, s:] == 0)
+        assert np.allclose(x[p, 4], np.log10(sg / 3.0), atol=1e-5)
+        assert np.allclose(x[p, 5], np.arange(L) / L)
+    fb = (rng.normal(size=N) + 1j * rng.normal(size=N)).astype(np.complex64)
+    pump = (rng.normal(size=N) + 1j * rng.normal(size=N)).astype(np.complex64)
+    tw = rng.uniform(size=N).astype(np.float32)
+    lin = np.exp(1j * rng.uniform(0, 2 * np.pi, N)).astype(np.complex64)
+    y = x[0, :4].copy()
+    e = torch.zeros(1, dtype=torch.float64, device=dev)
+    Xo = torch.empty(N, dtype=torch.complex64, device=dev)
+    Yn = ff.step(crop, torch.from_numpy(fb).to(dev), torch.from_numpy(pump).to(dev), torch.from_numpy(tw).to(dev),
+                 y=torch.from_numpy(y).to(dev), sigma=torch.tensor([sig[0]], device=dev),
+                 lin=torch.from_numpy(lin).to(dev), X_out=Xo, energy=e)
+    X = np.zeros(N, dtype=np.complex128)
+    X[idx] = Y[0, idx] * lin[idx]                      # decode(encode(Y)) is the crop of Y, times lin
+    assert np.allclose(Xo.cpu().numpy(), X, atol=1e-4)
+    assert np.allclose(Yn.cpu().numpy(), X * fb + pump, atol=1e-3)
+    ref_e = np.sum(tw * np.abs(X) ** 2)
+    assert abs(e.item() - ref_e) <= 1e-5 * ref_e
+
+
+def test_untrained_surrogate_falls_back_and_solver_finishes():
+    """An untrained network fails its first check; the solver takes over and the
+    trip accounting stays exact."""
+    from optifax_gb300 import fastforward as ff, opo
+    from optifax_gb300.surrogate import FNO
+    spec = opo.CavitySpec(crystal_length=0.5e-3)
+    crop = ff.reference_crop(spec)
+    net = FNO(n_bins=crop.n_bins, max_batch=1, seed=0)
+    sim = opo.OpticalSim(spec)
+    r = ff.run_fast_forward(sim, net, crop, max_trips=25, check_every=5, check_tol=0.05, finish_trips=5)
+    assert r["checks"] and not (r["checks"][0] <= 0.05)
+    assert r["fallback_blocks"] >= 1
+    assert r["trips"] == r["surrogate_trips"] + r["solver_trips"]
+    assert r["trips"] <= 25

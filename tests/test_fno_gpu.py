@@ -42,11 +42,12 @@ def test_fno_forward_backward_match_oracle(L, B):
     xg, tg = torch.from_numpy(x).to(dev), torch.from_numpy(t).to(dev)
     y = net.forward(xg).cpu().numpy()
     grads = torch.zeros(fo.N_PARAMS, dtype=torch.float32, device=dev)
-    loss = float(net.backward(xg, tg, grads).item())
+    sw = rng.uniform(0.5, 2.0, size=B).astype(np.float32)
+    loss = float(net.backward(xg, tg, grads, sample_w=torch.from_numpy(sw).to(dev)).item())
     g = grads.cpu().numpy()
     torch.cuda.synchronize()
     assert tc_error() == 0
-    lref, gref, yref = fo.loss_and_grads(p, x, t, weights_bf16=True)
+    lref, gref, yref = fo.loss_and_grads(p, x, t, weights_bf16=True, sample_w=sw)
     assert _rel(y, yref) <= Y_TOL
     assert abs(loss - lref) <= Y_TOL * lref
     bad = {n: _rel(g[a:b], gref[a:b]) for n, a, b in _blocks() if _rel(g[a:b], gref[a:b]) > G_TOL}
@@ -58,7 +59,7 @@ def test_fno_adam_reduces_loss():
     rng = np.random.default_rng(5)
     L, B = 256, 4
     net = FNO(n_bins=L, max_batch=B, params=init_params(1))
-    x = torch.from_numpy(rng.normal(size=(B, 5, L)).astype(np.float32)).to(net.dev)
+    x = torch.from_numpy(rng.normal(size=(B, 6, L)).astype(np.float32)).to(net.dev)
     tgt = x[:, :4] * 0.5 + 0.1
     l0 = float(net.backward(x, tgt.contiguous()).item())
     for _ in range(60):
