@@ -288,9 +288,9 @@ int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta2, float ep
  * band / sigma, 4 and 5 (if n_channels = 6) log10(sigma / pump_scale) and the bin
  * coordinate j / n_bins.  sigma is the RMS of the signal-band bins (written to
  * sigma_out) unless sigma_in supplies it.
- * optifax_ff_step: X = the decoded network output y[4][n_bins] (with sigma[0]) times
- * lin[k] (optional per-bin factor: the crystal's linear propagation, when the network
- * predicts the output in the interaction picture), or X_in when y is NULL; writes
+ * optifax_ff_step: X = the decoded network output y[4][n_bins] (with sigma[0]), or
+ * X_in when y is NULL, times lin[k] (optional per-bin factor: the crystal's linear
+ * propagation, when the network predicts the output in the interaction picture); writes
  * X_out (optional), Y_next = X feedback + pump and (optional) *energy = sum tally_w |X|^2
  * in FP64.  All pointers are device pointers.
  */
@@ -302,6 +302,24 @@ int optifax_ff_step(const float* y, const float* sigma, const void* X_in, const 
                     const void* pump, const void* lin, const float* tally_w, int32_t n_points,
                     int32_t k0, int32_t n_bins, int32_t split, float pump_scale, void* X_out,
                     void* Y_next, double* energy, void* stream);
+
+/*
+ * Envelope representation for the fast-forward (no reference counterpart).  band =
+ * {kc_pump, lo_pump, hi_pump, kc_signal, lo_signal, hi_signal} (HOST int32[6]): each
+ * band holds the bins whose signed offset o from its carrier bin kc lies in
+ * [lo, hi), |o| < n_bins / 2; its envelope is e_j = sum_o b_o exp(2 pi i o j / n_bins),
+ * j < n_bins (n_bins a power of two <= 4096).  optifax_ff_encode_env writes channels
+ * 0/1 = pump envelope / pump_scale, 2/3 = signal envelope / sigma (sigma = RMS of the
+ * signal envelope unless sigma_in is given), 4/5 (n_channels = 6) = log10(sigma /
+ * pump_scale) and j / n_bins.  optifax_ff_decode_env inverts channels 0-3 of one
+ * network output into the two bands of X_out (n_points complex, zero elsewhere).
+ */
+int optifax_ff_encode_env(const void* spectra, int64_t stride, int32_t n_spectra, int32_t n_points,
+                          int32_t n_bins, const int32_t* band, float pump_scale,
+                          const float* sigma_in, float* x, int32_t n_channels, float* sigma_out,
+                          void* stream);
+int optifax_ff_decode_env(const float* y, const float* sigma, int32_t n_points, int32_t n_bins,
+                          const int32_t* band, float pump_scale, void* X_out, void* stream);
 
 #ifdef __cplusplus
 }

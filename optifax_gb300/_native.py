@@ -19,7 +19,8 @@ EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifa
            "optifax_propagate_fp64", "optifax_gemm_bf16", "optifax_tc_error",
            "optifax_fno_param_count", "optifax_fno_create", "optifax_fno_destroy", "optifax_fno_set_params",
            "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
-           "optifax_ff_encode", "optifax_ff_step"]
+           "optifax_ff_encode", "optifax_ff_step",
+           "optifax_ff_encode_env", "optifax_ff_decode_env"]
 
 _lib = None
 
@@ -107,6 +108,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_ff_encode.restype = ctypes.c_int
     lib.optifax_ff_step.argtypes = [vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, f32, vp, vp, vp, vp]
     lib.optifax_ff_step.restype = ctypes.c_int
+    lib.optifax_ff_encode_env.argtypes = [vp, i64, i32, i32, i32, ctypes.POINTER(i32), f32, vp, vp, i32, vp, vp]
+    lib.optifax_ff_encode_env.restype = ctypes.c_int
+    lib.optifax_ff_decode_env.argtypes = [vp, vp, i32, i32, ctypes.POINTER(i32), f32, vp, vp]
+    lib.optifax_ff_decode_env.restype = ctypes.c_int
     _lib = lib
     return lib
 

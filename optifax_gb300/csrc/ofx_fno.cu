@@ -476,7 +476,7 @@ __global__ void k_ff_encode(const float2* __restrict__ Y, long long ystride, int
     }
 }
 
-// X = decoded network output times lin (or X_in); Y_next = X fb + pump; energy += sum tally_w |X|^2
+// X = (decoded network output or X_in) times lin; Y_next = X fb + pump; energy += sum tally_w |X|^2
 __global__ void k_ff_step(const float* __restrict__ y, const float* __restrict__ sigma, const float2* __restrict__ X_in,
                           const float2* __restrict__ fb, const float2* __restrict__ pump,
                           const float2* __restrict__ lin, const float* __restrict__ tw, int N, int k0, int L,
@@ -496,13 +496,13 @@ __global__ void k_ff_step(const float* __restrict__ y, const float* __restrict__
                 } else {
                     X = make_float2(y[j] * pump_scale, y[L + j] * pump_scale);
                 }
-                if (lin) {
-                    const float2 d = lin[k];
-                    X = make_float2(X.x * d.x - X.y * d.y, X.x * d.y + X.y * d.x);
-                }
             }
         } else {
             X = X_in[k];
+        }
+        if (lin) {
+            const float2 d = lin[k];
+            X = make_float2(X.x * d.x - X.y * d.y, X.x * d.y + X.y * d.x);
         }
         if (X_out) X_out[k] = X;
         const float2 f = fb[k], pp = pump[k];
@@ -518,6 +518,113 @@ __global__ void k_ff_step(const float* __restrict__ y, const float* __restrict__
             for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
             atomicAdd(energy, tot);
         }
+    }
+}
+
+// ---- OPO fast-forward, envelope representation ---------------------------
+// A band is the set of bins whose signed offset o from the band's carrier bin kc
+// (natural FFT order of the N-point spectrum) lies in [lo, hi), |o| < L/2.  Its
+// envelope is e_j = sum_o b_o exp(+2 pi i o j / L), j < L: the band demodulated to
+// its carrier and sampled L times over the window.
+struct EnvBand {
+    int kc, lo, hi;
+};
+
+__device__ __forceinline__ int env_bin(const EnvBand& b, int N, int L, int j, bool* in) {
+    const int o = j < L / 2 ? j : j - L;
+    *in = o >= b.lo && o < b.hi;
+    int k = (b.kc + o) % N;
+    return k < 0 ? k + N : k;
+}
+
+// in-place radix-2 DIT FFT of L points in shared memory (input already in
+// bit-reversed order); sign +1: exp(+2 pi i ...), -1: exp(-2 pi i ...)
+__device__ void smem_fft(float2* sm, int L, float sign) {
+    for (int len = 2; len <= L; len <<= 1) {
+        const int half = len >> 1;
+        for (int b = threadIdx.x; b < L / 2; b += blockDim.x) {
+            const int grp = b / half, j = b - grp * half;
+            const int i0 = grp * len + j, i1 = i0 + half;
+            float sn, cs;
+            sincospif(sign * 2.f * (float)j / (float)len, &sn, &cs);
+            const float2 u = sm[i0], v0 = sm[i1];
+            const float2 v = make_float2(v0.x * cs - v0.y * sn, v0.x * sn + v0.y * cs);
+            sm[i0] = make_float2(u.x + v.x, u.y + v.y);
+            sm[i1] = make_float2(u.x - v.x, u.y - v.y);
+        }
+        __syncthreads();
+    }
+}
+
+// grid (spectra, 2 bands): envelopes -> channels 0/1 (pump / pump_scale), 2/3
+// (signal / sigma), 4 log10(sigma / pump_scale), 5 j / L
+__global__ void k_ff_encode_env(const float2* __restrict__ Y, long long ystride, int N, int L, int logL, EnvBand bp,
+                                EnvBand bs, float pump_scale, const float* __restrict__ sigma_in,
+                                float* __restrict__ x, int nch, float* __restrict__ sigma_out) {
+    __shared__ float2 sm[4096];
+    __shared__ float red[32];
+    __shared__ float s_sig;
+    const int p = blockIdx.x, band = blockIdx.y;
+    const EnvBand bd = band ? bs : bp;
+    const float2* y = Y + p * ystride;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        bool in;
+        const int k = env_bin(bd, N, L, j, &in);
+        sm[__brev((unsigned)j) >> (32 - logL)] = in ? y[k] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    smem_fft(sm, L, 1.f);
+    float scale = 1.f / pump_scale, sg = 1.f;
+    if (band == 1) {
+        if (sigma_in) {
+            if (threadIdx.x == 0) s_sig = sigma_in[p];
+        } else {
+            float acc = 0.f;
+            for (int j = threadIdx.x; j < L; j += blockDim.x) acc = fmaf(sm[j].x, sm[j].x, fmaf(sm[j].y, sm[j].y, acc));
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                float tot = 0.f;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += red[w];
+                float v = sqrtf(tot / (float)L);
+                const float floor_ = 1e-30f * pump_scale;
+                if (!(v > floor_)) v = floor_;
+                s_sig = v;
+                if (sigma_out) sigma_out[p] = v;
+            }
+        }
+        __syncthreads();
+        sg = s_sig;
+        scale = 1.f / sg;
+    }
+    float* xo = x + (long long)p * nch * L;
+    const float lg = log10f(sg / pump_scale);
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        xo[(2 * band) * L + j] = sm[j].x * scale;
+        xo[(2 * band + 1) * L + j] = sm[j].y * scale;
+        if (band == 1 && nch > 4) {
+            xo[4 * L + j] = lg;
+            xo[5 * L + j] = (float)j / (float)L;
+        }
+    }
+}
+
+// grid (2 bands): network output envelopes -> band bins of X (X zeroed by the host)
+__global__ void k_ff_decode_env(const float* __restrict__ y, const float* __restrict__ sigma, int N, int L, int logL,
+                                EnvBand bp, EnvBand bs, float pump_scale, float2* __restrict__ X) {
+    __shared__ float2 sm[4096];
+    const int band = blockIdx.x;
+    const EnvBand bd = band ? bs : bp;
+    for (int j = threadIdx.x; j < L; j += blockDim.x)
+        sm[__brev((unsigned)j) >> (32 - logL)] = make_float2(y[(2 * band) * L + j], y[(2 * band + 1) * L + j]);
+    __syncthreads();
+    smem_fft(sm, L, -1.f);
+    const float scale = (band ? sigma[0] : pump_scale) / (float)L;
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        bool in;
+        const int k = env_bin(bd, N, L, j, &in);
+        if (in) X[k] = make_float2(sm[j].x * scale, sm[j].y * scale);
     }
 }
 
@@ -770,5 +877,51 @@ extern "C" int optifax_ff_step(const float* y, const float* sigma, const void* X
                                               static_cast<const float2*>(lin), tally_w, n_points, k0, n_bins, split,
                                               pump_scale, static_cast<float2*>(X_out), static_cast<float2*>(Y_next),
                                               energy);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+namespace {
+int env_args(int32_t n_points, int32_t n_bins, const int32_t* band, EnvBand* bp, EnvBand* bs, int* logL) {
+    if (!band || n_points < 1 || n_bins < 2 || n_bins > 4096 || (n_bins & (n_bins - 1)) || n_bins > n_points)
+        return OPTIFAX_ERR_INVALID_ARGUMENT;
+    *bp = {band[0], band[1], band[2]};
+    *bs = {band[3], band[4], band[5]};
+    for (const EnvBand* b : {bp, bs})
+        if (b->kc < 0 || b->kc >= n_points || b->lo < -n_bins / 2 || b->hi > n_bins / 2 || b->lo >= b->hi)
+            return OPTIFAX_ERR_INVALID_ARGUMENT;
+    int l = 0;
+    while ((1 << l) < n_bins) ++l;
+    *logL = l;
+    return OPTIFAX_OK;
+}
+}  // namespace
+
+extern "C" int optifax_ff_encode_env(const void* spectra, int64_t stride, int32_t n_spectra, int32_t n_points,
+                                     int32_t n_bins, const int32_t* band, float pump_scale, const float* sigma_in,
+                                     float* x, int32_t n_channels, float* sigma_out, void* stream) {
+    EnvBand bp, bs;
+    int logL = 0;
+    if (!spectra || !x || n_spectra < 1 || stride < n_points || !(pump_scale > 0.f) ||
+        (n_channels != 4 && n_channels != 6))
+        return OPTIFAX_ERR_INVALID_ARGUMENT;
+    int rc = env_args(n_points, n_bins, band, &bp, &bs, &logL);
+    if (rc) return rc;
+    k_ff_encode_env<<<dim3(n_spectra, 2), 512, 0, static_cast<cudaStream_t>(stream)>>>(
+        static_cast<const float2*>(spectra), stride, n_points, n_bins, logL, bp, bs, pump_scale, sigma_in, x,
+        n_channels, sigma_out);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+extern "C" int optifax_ff_decode_env(const float* y, const float* sigma, int32_t n_points, int32_t n_bins,
+                                     const int32_t* band, float pump_scale, void* X_out, void* stream) {
+    EnvBand bp, bs;
+    int logL = 0;
+    if (!y || !sigma || !X_out || !(pump_scale > 0.f)) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    int rc = env_args(n_points, n_bins, band, &bp, &bs, &logL);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(X_out, 0, sizeof(float2) * (size_t)n_points, st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    k_ff_decode_env<<<2, 512, 0, st>>>(y, sigma, n_points, n_bins, logL, bp, bs, pump_scale,
+                                       static_cast<float2*>(X_out));
     return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
 }

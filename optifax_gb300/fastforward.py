@@ -24,6 +24,7 @@ output X_t) with Y_0 = FFT(E_0) and Y_{t+1} = X_t feedback + pump.
 """
 from __future__ import annotations
 
+import ctypes
 import dataclasses
 import math
 import time
@@ -69,6 +70,59 @@ def reference_crop(spec: Optional[opo.CavitySpec] = None) -> Crop:
     return make_crop(a.win, float(np.max(np.abs(a.pump))))
 
 
+@dataclasses.dataclass
+class EnvCrop:
+    """Envelope representation: each band demodulated to its carrier and sampled
+    n_bins times over the window (time-domain channels).  band = (kc_pump, lo_pump,
+    hi_pump, kc_signal, lo_signal, hi_signal): carrier bins (natural FFT order) and
+    the signed bin-offset range of each band."""
+
+    n_points: int
+    n_bins: int
+    band: tuple
+    pump_scale: float
+
+
+def envelope(spectrum: np.ndarray, kc: int, lo: int, hi: int, n_bins: int) -> np.ndarray:
+    """e_j = sum_{o in [lo, hi)} X[(kc + o) mod N] exp(2 pi i o j / n_bins) (host, FP64)."""
+    n = spectrum.shape[-1]
+    b = np.zeros(n_bins, dtype=np.complex128)
+    o = np.arange(lo, hi)
+    b[o % n_bins] = spectrum[(kc + o) % n]
+    return n_bins * np.fft.ifft(b)
+
+
+def make_env_crop(win, pump_k: np.ndarray, n_bins: int = N_BINS, f_lo: float = F_LO, f_split: float = F_SPLIT,
+                  signal_band_nm=(1350.0, 1800.0), pump_wavelength: Optional[float] = None) -> EnvCrop:
+    n = win.n_points
+    df = 1.0 / (n * win.dt)
+    f0 = win.f0
+    rel = lambda f: (f - f0) / df
+    split_rel = int(math.ceil(rel(f_split)))
+    lo_rel = int(math.ceil(rel(f_lo)))
+    kc_p = int(round(rel(opo.ph.C0 / (pump_wavelength or win.reference_wave))))
+    f_s = 0.5 * (opo.ph.C0 / (signal_band_nm[1] * 1e-9) + opo.ph.C0 / (signal_band_nm[0] * 1e-9))
+    kc_s = int(round(rel(f_s)))
+    lo_p, hi_p = split_rel - kc_p, n_bins // 2
+    lo_s, hi_s = lo_rel - kc_s, split_rel - kc_s
+    if not (-n_bins // 2 <= lo_p < hi_p <= n_bins // 2 and -n_bins // 2 <= lo_s < hi_s <= n_bins // 2):
+        raise ValueError("bands do not fit the envelope grid")
+    band = (kc_p % n, lo_p, hi_p, kc_s % n, lo_s, hi_s)
+    scale = float(np.max(np.abs(envelope(np.asarray(pump_k), band[0], lo_p, hi_p, n_bins))))
+    return EnvCrop(n, n_bins, band, scale)
+
+
+def reference_env_crop(spec: Optional[opo.CavitySpec] = None) -> EnvCrop:
+    spec = spec or opo.CavitySpec()
+    ref = dataclasses.replace(spec, pump_power=2.0, pump_tau=200e-15)
+    a = opo.build_cavity(ref)
+    return make_env_crop(a.win, a.pump, signal_band_nm=spec.signal_band_nm, pump_wavelength=spec.pump_wavelength)
+
+
+def _band(crop: EnvCrop):
+    return (ctypes.c_int32 * 6)(*[int(v) for v in crop.band])
+
+
 def _ptr(t):
     return t.data_ptr() if t is not None else None
 
@@ -77,13 +131,19 @@ def _stream(dev):
     return int(torch.cuda.current_stream(dev).cuda_stream)
 
 
-def encode(spectra: torch.Tensor, crop: Crop, sigma_in: Optional[torch.Tensor] = None, n_channels: int = CIN):
+def encode(spectra: torch.Tensor, crop, sigma_in: Optional[torch.Tensor] = None, n_channels: int = CIN):
     """(P, N) complex64 spectra -> (x (P, n_channels, n_bins) float32, sigma (P,))."""
     spectra = spectra.contiguous()
     P = spectra.shape[0]
     dev = spectra.device
     x = torch.empty((P, n_channels, crop.n_bins), dtype=torch.float32, device=dev)
     sig = sigma_in.contiguous() if sigma_in is not None else torch.empty(P, dtype=torch.float32, device=dev)
+    if isinstance(crop, EnvCrop):
+        rc = nat.load().optifax_ff_encode_env(spectra.data_ptr(), spectra.stride(0), P, crop.n_points, crop.n_bins,
+                                              _band(crop), crop.pump_scale, _ptr(sigma_in), x.data_ptr(), n_channels,
+                                              None if sigma_in is not None else sig.data_ptr(), _stream(dev))
+        nat.check(rc, None, "optifax_ff_encode_env")
+        return x, sig
     rc = nat.load().optifax_ff_encode(spectra.data_ptr(), spectra.stride(0), P, crop.n_points, crop.k0,
                                       crop.n_bins, crop.split, crop.pump_scale,
                                       _ptr(sigma_in), x.data_ptr(), n_channels,
@@ -92,15 +152,32 @@ def encode(spectra: torch.Tensor, crop: Crop, sigma_in: Optional[torch.Tensor] =
     return x, sig
 
 
-def step(crop: Crop, feedback, pump, tally_w, *, y=None, sigma=None, lin=None, X_in=None, X_out=None,
+def decode_env(crop: EnvCrop, y: torch.Tensor, sigma: torch.Tensor, X_out: Optional[torch.Tensor] = None):
+    """One network output (1, 4, n_bins) -> the two bands of an N-point spectrum."""
+    if X_out is None:
+        X_out = torch.empty(crop.n_points, dtype=torch.complex64, device=y.device)
+    rc = nat.load().optifax_ff_decode_env(y.contiguous().data_ptr(), sigma.data_ptr(), crop.n_points, crop.n_bins,
+                                          _band(crop), crop.pump_scale, X_out.data_ptr(), _stream(y.device))
+    nat.check(rc, None, "optifax_ff_decode_env")
+    return X_out
+
+
+def step(crop, feedback, pump, tally_w, *, y=None, sigma=None, lin=None, X_in=None, X_out=None,
          Y_next=None, energy=None):
-    """X from the network output y (decoded with sigma, times lin) or X_in; returns
+    """X from the network output y (decoded with sigma) or X_in, times lin; returns
     Y_next = X fb + pump (and fills energy = sum tally_w |X|^2 when given)."""
     dev = feedback.device
     if Y_next is None:
         Y_next = torch.empty(crop.n_points, dtype=torch.complex64, device=dev)
+    if isinstance(crop, EnvCrop):
+        if y is not None:
+            X_in = decode_env(crop, y, sigma)
+            y = sigma = None
+        k0, nb, split = 0, crop.n_bins, 0
+    else:
+        k0, nb, split = crop.k0, crop.n_bins, crop.split
     rc = nat.load().optifax_ff_step(_ptr(y), _ptr(sigma), _ptr(X_in), feedback.data_ptr(), pump.data_ptr(),
-                                    _ptr(lin), _ptr(tally_w), crop.n_points, crop.k0, crop.n_bins, crop.split,
+                                    _ptr(lin), _ptr(tally_w), crop.n_points, k0, nb, split,
                                     crop.pump_scale, _ptr(X_out), Y_next.data_ptr(), _ptr(energy), _stream(dev))
     nat.check(rc, None, "optifax_ff_step")
     return Y_next
@@ -134,12 +211,12 @@ def training_specs(n: int, seed: int = 3, power=(0.5, 3.0), tau=(100e-15, 300e-1
                                 seed=seed * 100000 + i) for i in range(n)]
 
 
-def generate_pairs(specs: List[opo.CavitySpec], n_trips: int, crop: Crop, device: int = 0, group: int = 38):
-    """Run the cavities (group at a time, one launch per group) and return the
-    encoded pairs (x (P, 6, L), interaction-picture target (P, 4, L)), the trip
-    index of every pair and the solver attempt count."""
+def generate_raw(specs: List[opo.CavitySpec], n_trips: int, device: int = 0, group: int = 38):
+    """Run the cavities (group at a time, one launch per group) and return the raw
+    pairs: crystal-input spectra (P, N), interaction-picture crystal-output spectra
+    (P, N), the trip index of every pair and the solver attempt count."""
     dev = torch.device(f"cuda:{device}")
-    xs, ts, trip_idx = [], [], []
+    ins_all, outs_all, trip_idx = [], [], []
     attempts = 0
     for g0 in range(0, len(specs), group):
         sims = [opo.OpticalSim(s, device=device) for s in specs[g0:g0 + group]]
@@ -152,13 +229,30 @@ def generate_pairs(specs: List[opo.CavitySpec], n_trips: int, crop: Crop, device
             ins[0] = y0
             if hist.shape[0] > 1:
                 ins[1:] = hist[:-1] * sim.feedback + sim.pump
-            x, sig = encode(ins, crop)
-            t, _ = encode(to_interaction(hist, linear_factor(sim)), crop, sigma_in=sig, n_channels=COUT)
-            xs.append(x)
-            ts.append(t)
+            ins_all.append(ins)
+            outs_all.append(to_interaction(hist, linear_factor(sim)))
             trip_idx.append(torch.arange(hist.shape[0]))
         del sims, res
-    return torch.cat(xs), torch.cat(ts), torch.cat(trip_idx), attempts
+    return torch.cat(ins_all), torch.cat(outs_all), torch.cat(trip_idx), attempts
+
+
+def encode_pairs(ins: torch.Tensor, outs: torch.Tensor, crop, chunk: int = 1024):
+    """Network inputs (P, 6, L) and targets (P, 4, L) of raw pairs (targets scaled
+    with the input's sigma)."""
+    xs, ts = [], []
+    for i in range(0, ins.shape[0], chunk):
+        x, sig = encode(ins[i:i + chunk], crop)
+        t, _ = encode(outs[i:i + chunk], crop, sigma_in=sig, n_channels=COUT)
+        xs.append(x)
+        ts.append(t)
+    return torch.cat(xs), torch.cat(ts)
+
+
+def generate_pairs(specs: List[opo.CavitySpec], n_trips: int, crop, device: int = 0, group: int = 38):
+    """generate_raw + encode_pairs: (x, target, trip index, solver attempts)."""
+    ins, outs, trip_idx, attempts = generate_raw(specs, n_trips, device, group)
+    X, T = encode_pairs(ins, outs, crop)
+    return X, T, trip_idx, attempts
 
 
 def signal_rel_err(y: torch.Tensor, t: torch.Tensor) -> torch.Tensor:
@@ -219,11 +313,16 @@ def train(net: FNO, X: torch.Tensor, T: torch.Tensor, *, epochs: int = 40, batch
     hist["steps"] = step_i
     ve = evaluate(net, X[vdev], T[vdev]).cpu()
     hist["val_signal_rel_l2_quantiles"] = [float(v) for v in torch.quantile(ve, torch.tensor([0.1, 0.5, 0.9]))]
+    # the same error for the identity map (output = input in the interaction picture)
+    ident = signal_rel_err(X[vdev][:, :COUT], T[vdev]).cpu()
+    hist["val_identity_rel_l2_median"] = float(ident.median())
     if trip_idx is not None:
         ti = trip_idx[val]
         bins = [(0, 20), (20, 60), (60, 10 ** 9)]
         hist["val_by_trip"] = {f"{a}-{b}": float(ve[(ti >= a) & (ti < b)].median())
                                for a, b in bins if bool(((ti >= a) & (ti < b)).any())}
+        hist["val_identity_by_trip"] = {f"{a}-{b}": float(ident[(ti >= a) & (ti < b)].median())
+                                        for a, b in bins if bool(((ti >= a) & (ti < b)).any())}
     return hist
 
 
@@ -241,7 +340,7 @@ def _to_spec(E: torch.Tensor) -> torch.Tensor:
     return torch.from_numpy(np.fft.fft(E.cpu().numpy().astype(np.complex128)).astype(np.complex64)).to(E.device)
 
 
-def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop: Crop, *, max_trips: int = 1000,
+def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips: int = 1000,
                      check_every: int = 10, check_tol: float = 0.05, finish_trips: int = 50,
                      flat_tol: float = 1e-3, steady_tol: float = 1e-4, steady_trips: int = 10) -> dict:
     """max_trips round trips from sim's current state.

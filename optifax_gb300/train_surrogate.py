@@ -1,10 +1,11 @@
 """Train the crystal-pass surrogate on solver-generated pairs, then time the OPO with it.
 
-    python -m optifax_gb300.train_surrogate --cavities 38 --trips 160 --epochs 120 --out DIR
+    python -m optifax_gb300.train_surrogate --cavities 38 --trips 160 --epochs 120 --repr env --out DIR
 
-Writes DIR/fno_params.npy (the FP32 parameter vector) and DIR/train_summary.json
-(data generation and training figures, the fast-forward OPO run against the
-solver-only run and the plain FP64 solver's trip rate).
+Writes DIR/fno_params_<repr>.npy (the FP32 parameter vector of each trained
+representation) and DIR/train_summary.json (data generation and training figures,
+the identity-map baseline, the fast-forward OPO runs, optionally the solver-only
+run, and the plain FP64 solver's trip rate).
 """
 from __future__ import annotations
 
@@ -26,56 +27,62 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--crystal-length", type=float, default=5e-3)
-    ap.add_argument("--eval-trips", type=int, default=200)
+    ap.add_argument("--repr", default="env", help="comma list of representations: env (band envelopes), bins")
+    ap.add_argument("--eval-trips", type=int, default=100)
+    ap.add_argument("--solver-only-trips", type=int, default=0)
     ap.add_argument("--check-tol", type=float, default=0.05)
-    ap.add_argument("--fp64-trips", type=int, default=2)
-    ap.add_argument("--no-eval", action="store_true")
+    ap.add_argument("--fp64-trips", type=int, default=1)
     ap.add_argument("--out", default="surrogate_out")
     args = ap.parse_args(argv)
     from . import fastforward as ff, opo
     from .surrogate import FNO
     os.makedirs(args.out, exist_ok=True)
-    summary = {"args": vars(args)}
+    summary = {"args": vars(args), "runs": {}}
     base = opo.CavitySpec(crystal_length=args.crystal_length)
-    crop = ff.reference_crop(base)
-    summary["crop"] = {"k0": crop.k0, "n_bins": crop.n_bins, "split": crop.split, "pump_scale": crop.pump_scale}
     t0 = time.perf_counter()
     specs = ff.training_specs(args.cavities, seed=args.seed, base=base)
-    X, T, trip_idx, attempts = ff.generate_pairs(specs, args.trips, crop)
+    ins, outs, trip_idx, attempts = ff.generate_raw(specs, args.trips)
     torch.cuda.synchronize()
-    summary["generation"] = {"pairs": int(X.shape[0]), "seconds": time.perf_counter() - t0,
+    summary["generation"] = {"pairs": int(ins.shape[0]), "seconds": time.perf_counter() - t0,
                              "solver_attempts": attempts}
     print(json.dumps(summary["generation"]), flush=True)
-    net = FNO(n_bins=crop.n_bins, max_batch=args.batch, seed=args.seed)
-    hist = ff.train(net, X, T, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed,
-                    trip_idx=trip_idx, log=lambda s: print(s, flush=True))
-    summary["training"] = hist
-    print(json.dumps({k: hist[k] for k in ("seconds", "steps", "val_signal_rel_l2_quantiles")
-                      + (("val_by_trip",) if "val_by_trip" in hist else ())}), flush=True)
-    params = net.params().cpu().numpy()
-    np.save(os.path.join(args.out, "fno_params.npy"), params)
-    del X, T
-    torch.cuda.empty_cache()
-    if not args.no_eval:
-        spec = base                       # the evaluation cavity: 2 W, 200 fs, noise seed 1
-        infer = FNO(n_bins=crop.n_bins, max_batch=1, params=params)
-        solo = ff.run_fast_forward(opo.OpticalSim(spec), None, crop, max_trips=args.eval_trips)
-        fast = ff.run_fast_forward(opo.OpticalSim(spec), infer, crop, max_trips=args.eval_trips,
-                                   check_tol=args.check_tol)
-        fp64 = ff.fp64_plain_trips(spec, args.fp64_trips)
+    for rep in [r.strip() for r in args.repr.split(",") if r.strip()]:
+        crop = ff.reference_env_crop(base) if rep == "env" else ff.reference_crop(base)
+        X, T = ff.encode_pairs(ins, outs, crop)
+        net = FNO(n_bins=crop.n_bins, max_batch=args.batch, seed=args.seed)
+        hist = ff.train(net, X, T, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed,
+                        trip_idx=trip_idx, log=lambda s: print(f"[{rep}] {s}", flush=True))
+        run = {"training": hist}
+        print(json.dumps({"repr": rep, **{k: hist[k] for k in hist if k not in ("train_loss", "val_signal_rel_l2")}}),
+              flush=True)
+        params = net.params().cpu().numpy()
+        np.save(os.path.join(args.out, f"fno_params_{rep}.npy"), params)
+        del X, T, net
+        torch.cuda.empty_cache()
+        if args.eval_trips > 0:
+            infer = FNO(n_bins=crop.n_bins, max_batch=1, params=params)
+            fast = ff.run_fast_forward(opo.OpticalSim(base), infer, crop, max_trips=args.eval_trips,
+                                       check_tol=args.check_tol)
+            fast.pop("field")
+            fast["energies"] = fast["energies"][-10:]
+            run["fast_forward"] = fast
+            print(json.dumps({"repr": rep, "fast_forward": {k: fast[k] for k in
+                                                            ("trips", "surrogate_trips", "solver_trips",
+                                                             "fallback_blocks", "wall_s", "trips_per_s")},
+                              "checks": fast["checks"]}), flush=True)
+            del infer
+        summary["runs"][rep] = run
+    if args.solver_only_trips > 0:
+        solo = ff.run_fast_forward(opo.OpticalSim(base), None, ff.reference_crop(base),
+                                   max_trips=args.solver_only_trips)
+        solo.pop("field")
+        solo["energies"] = solo["energies"][-10:]
+        summary["solver_only"] = solo
+    if args.fp64_trips > 0:
+        fp64 = ff.fp64_plain_trips(base, args.fp64_trips)
         fp64.pop("field")
-        a_s, a_f = solo.pop("field"), fast.pop("field")
-        for r in (solo, fast):
-            r["energies_head"] = r["energies"][:60:3]
-            r["energies"] = r["energies"][-20:]
-        summary["eval"] = {"solver_only": solo, "surrogate_plus_solver": fast, "fp64_plain": fp64,
-                           "field_rel_l2_vs_solver_only": float((a_f - a_s).norm() / a_s.norm()),
-                           "speedup_vs_fp64_plain": fast["trips_per_s"] / fp64["trips_per_s"],
-                           "speedup_vs_solver_only_wall": solo["wall_s"] / fast["wall_s"],
-                           "final_energy_rel_diff": abs(fast["final_output_signal_energy"] -
-                                                        solo["final_output_signal_energy"]) /
-                           abs(solo["final_output_signal_energy"])}
-        print(json.dumps(summary["eval"], default=float), flush=True)
+        summary["fp64_plain"] = fp64
+        print(json.dumps({"fp64_plain": fp64}), flush=True)
     with open(os.path.join(args.out, "train_summary.json"), "w") as f:
         json.dump(summary, f, indent=1, default=float)
 

@@ -58,3 +58,31 @@ def test_untrained_surrogate_falls_back_and_solver_finishes():
     assert r["fallback_blocks"] >= 1
     assert r["trips"] == r["surrogate_trips"] + r["solver_trips"]
     assert r["trips"] <= 25
+
+
+def test_envelope_encode_decode_round_trip():
+    from optifax_gb300 import fastforward as ff, opo
+    spec = opo.CavitySpec()
+    a = opo.build_cavity(spec)
+    crop = ff.reference_env_crop(spec)
+    kp, lop, hip, ks, los, his = crop.band
+    rng = np.random.default_rng(1)
+    N, L = crop.n_points, crop.n_bins
+    Y = (rng.normal(size=(2, N)) + 1j * rng.normal(size=(2, N))).astype(np.complex64)
+    dev = torch.device("cuda:0")
+    x, sig = ff.encode(torch.from_numpy(Y).to(dev), crop)
+    xh, sg = x.cpu().numpy(), sig.cpu().numpy()
+    for p in range(2):
+        ep = ff.envelope(Y[p].astype(np.complex128), kp, lop, hip, L)
+        es = ff.envelope(Y[p].astype(np.complex128), ks, los, his, L)
+        s = np.sqrt(np.mean(np.abs(es) ** 2))
+        assert abs(sg[p] - s) <= 1e-4 * s
+        assert np.abs(xh[p, 0] + 1j * xh[p, 1] - ep / crop.pump_scale).max() <= 1e-4 * np.abs(ep).max() / crop.pump_scale
+        assert np.abs(xh[p, 2] + 1j * xh[p, 3] - es / s).max() <= 1e-4 * np.abs(es).max() / s
+        assert np.allclose(xh[p, 5], np.arange(L) / L)
+    X = ff.decode_env(crop, x[0:1, :4].contiguous(), sig[0:1]).cpu().numpy()
+    ref = np.zeros(N, dtype=np.complex128)
+    for kc, lo, hi in ((kp, lop, hip), (ks, los, his)):
+        idx = (kc + np.arange(lo, hi)) % N
+        ref[idx] = Y[0, idx]
+    assert np.abs(X - ref).max() <= 1e-4 * np.abs(ref).max()
