@@ -49,7 +49,9 @@ typedef enum {
     OPTIFAX_VARIANT_BATCH_OP = 1,   /* as XTAL with one G shared by all pulses (OPO_CUDA_BATCH_OP.cu:221) */
     OPTIFAX_VARIANT_NO_BC = 2,      /* unshifted time, no absorber, truncated chunk count (OPO_CUDA_NO_BC.cu) */
     OPTIFAX_VARIANT_HARD_BC = 3,    /* unshifted time, hard absorber (OPO_CUDA_HARD_BC.cu:118-129) */
-    OPTIFAX_VARIANT_ODE23 = 4       /* unshifted time, sech^2 absorber, truncated chunks, shared G (OPO_CUDA_ODE23.cu) */
+    OPTIFAX_VARIANT_ODE23 = 4,      /* unshifted time, sech^2 absorber, truncated chunks, shared G (OPO_CUDA_ODE23.cu) */
+    OPTIFAX_VARIANT_NEE = 5         /* NEE_CPU.m:1-122 (Heun): fftshift(t), t-based absorber, 1-based G, reject keeps k,
+                                       grow below minErr, clamp only at the crystal end, snapshot fft(A) per chunk */
 } optifax_variant;
 
 /* Per-pulse status bits returned in optifax_pulse_stats.status. */
@@ -222,7 +224,8 @@ int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t variant,
  * n_pulses x n_steps when g_per_pulse.  All pulses share one step schedule (the
  * reference's batch rule).  trace_host (optional, HOST, 3 x trace_cap int32):
  * per attempt {k, stepmod, flags | 8 if accepted}; stats_host (optional, HOST).
- * Variant ODE23 is not offered.  Calls on one device are serialised internally.
+ * Variant ODE23 is not offered; NEE follows NEE_CPU.m (the snapshot outputs are not
+ * produced by this entry).  Calls on one device are serialised internally.
  */
 int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_t n_steps,
                            const double* E_in, double* A_out, const double* alpha,

@@ -11,7 +11,7 @@ import os
 from . import build as _build
 
 HEUN, RK23 = 0, 1
-VARIANT_BATCH_XTAL, VARIANT_BATCH_OP, VARIANT_NO_BC, VARIANT_HARD_BC, VARIANT_ODE23 = range(5)
+VARIANT_BATCH_XTAL, VARIANT_BATCH_OP, VARIANT_NO_BC, VARIANT_HARD_BC, VARIANT_ODE23, VARIANT_NEE = range(6)
 PULSE_NAN, PULSE_ATTEMPT_LIMIT = 0x1, 0x2
 
 EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifax_last_error",

@@ -130,7 +130,7 @@ const KernelEntry* find_kernel(int M, int C, int method) {
     return nullptr;
 }
 
-struct VariantCfg { int time_mode, abc_mode, guard, g_per_pulse, stepmods_rule; };
+struct VariantCfg { int time_mode, abc_mode, guard, g_per_pulse, stepmods_rule, nee = 0; };
 
 bool variant_cfg(int variant, VariantCfg* v) {
     switch (variant) {
@@ -139,6 +139,7 @@ bool variant_cfg(int variant, VariantCfg* v) {
         case OPTIFAX_VARIANT_NO_BC:      *v = {TIME_UNSHIFTED, ABC_NONE, 0, 0, 128}; return true;
         case OPTIFAX_VARIANT_HARD_BC:    *v = {TIME_UNSHIFTED, ABC_HARD, 0, 0, 128}; return true;
         case OPTIFAX_VARIANT_ODE23:      *v = {TIME_UNSHIFTED, ABC_SOFT, 0, 0, 256}; return true;
+        case OPTIFAX_VARIANT_NEE:        *v = {TIME_NEE, ABC_NEE, 0, 0, 128, 1}; return true;
         default: return false;
     }
 }
@@ -266,6 +267,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         cfg.shared_sched = shared ? 1 : 0;
         cfg.max_attempts_mul = 64;
         cfg.grid_flags = h->d_grid_flags;
+        cfg.nee = vc.nee;
         cudaStream_t ls = st;
         if (gi > 0) {
             ls = h->side[gi - 1];
@@ -422,6 +424,8 @@ int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_p
         return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown method");
     VariantCfg vc;
     if (!variant_cfg(variant, &vc)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown variant");
+    if (vc.nee && method != OPTIFAX_HEUN)
+        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "the NEE variant is a Heun schedule (NEE_CPU.m)");
     if (cta_points != 0 && (!is_pow2(cta_points) || cta_points < 512 || cta_points > 4096))
         return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "cta_points must be 0 or a power of two in [512, 4096]");
     cudaError_t e = cudaSetDevice(h->device);

@@ -35,6 +35,7 @@ __device__ __forceinline__ double2 dmul(double2 a, double2 b) {
 
 __device__ __forceinline__ double sample_time(int mode, int i, int n, double dt) {
     if (mode == 0) return (i > n / 2) ? dt * (double)(i - n / 2) : dt * (double)(i + n / 2);
+    if (mode == 2) return (i < n / 2) ? dt * (double)i : dt * (double)(i - n);    // fftshift(t) (NEE)
     return dt * (double)i;
 }
 
@@ -58,7 +59,7 @@ __global__ void f64_nl(const double2* __restrict__ X, double2* __restrict__ NL, 
 // mode 1: E = A0 + (K/2 + K1/2), class |E - (A0 + K1)| against the thresholds
 __global__ void f64_k(const double2* __restrict__ NL, const double2* __restrict__ A0, double2* __restrict__ K1,
                       double2* __restrict__ X, const double* __restrict__ G, int gstride, int kidx, double hmod,
-                      double cs, int n, int mode, double maxE, double minE, int* flags) {
+                      double cs, int n, int mode, double maxE, double minE, int nee, int* flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int b = blockIdx.y;
@@ -74,12 +75,22 @@ __global__ void f64_k(const double2* __restrict__ NL, const double2* __restrict_
         X[base + i] = make_double2(a0.x + (0.5 * k.x + 0.5 * k.x), a0.y + (0.5 * k.y + 0.5 * k.y));
     } else {
         double2 k1 = K1[base + i];
-        double2 e = make_double2(a0.x + (0.5 * k.x + 0.5 * k1.x), a0.y + (0.5 * k.y + 0.5 * k1.y));
-        double2 a1 = make_double2(a0.x + (0.5 * k1.x + 0.5 * k1.x), a0.y + (0.5 * k1.y + 0.5 * k1.y));
+        double2 e, a1;
+        if (nee) {    // NEE_CPU.m:73-75: A1 = A0 + K1, E = (A0 + K1/2) + K2/2
+            e = make_double2((a0.x + 0.5 * k1.x) + 0.5 * k.x, (a0.y + 0.5 * k1.y) + 0.5 * k.y);
+            a1 = make_double2(a0.x + k1.x, a0.y + k1.y);
+        } else {
+            e = make_double2(a0.x + (0.5 * k.x + 0.5 * k1.x), a0.y + (0.5 * k.y + 0.5 * k1.y));
+            a1 = make_double2(a0.x + (0.5 * k1.x + 0.5 * k1.x), a0.y + (0.5 * k1.y + 0.5 * k1.y));
+        }
         X[base + i] = e;
         double ae = hypot(e.x, e.y);
         int bits = 0;
-        if (ae > 0.0) {
+        if (nee) {    // every point; maxErr strict (NEE_CPU.m:77-79)
+            double pct = 100.0 * hypot(e.x - a1.x, e.y - a1.y) / (ae + 1.0);
+            if (pct > maxE) bits |= 1;
+            if (pct >= minE) bits |= 2;
+        } else if (ae > 0.0) {
             double pct = 100.0 * hypot(e.x - a1.x, e.y - a1.y) / (ae + 1.0);
             if (pct >= maxE) bits = 1;
             else if (pct >= minE) bits = 2;
@@ -90,9 +101,17 @@ __global__ void f64_k(const double2* __restrict__ NL, const double2* __restrict_
     }
 }
 
-__global__ void f64_abc(double2* X, int n, int abc_mode) {
+__global__ void f64_abc(double2* X, int n, int abc_mode, double dt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || abc_mode == 1) return;
+    if (abc_mode == 3) {    // NEE_CPU.m:114-121
+        const double t = sample_time(2, i, n, dt), range = (double)(n - 1) * dt, a2t = fabs(2.0 * t);
+        if (!(range - a2t < 0.25 * range)) return;
+        const double sh = 1.0 / cosh(24.0 * (1.0 - a2t / range));
+        const size_t o = (size_t)blockIdx.y * n + i;
+        X[o] = make_double2(X[o].x * (1.0 - sh * sh), X[o].y * (1.0 - sh * sh));
+        return;
+    }
     int gi1 = 6 * (n / 16), gi2 = 10 * (n / 16);
     if (!(i > gi1 && i < gi2)) return;
     size_t o = (size_t)blockIdx.y * n + i;
@@ -219,12 +238,13 @@ extern "C" int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_
     const int n = n_points, B = n_pulses, S = n_steps;
     if (n < 16 || (n & (n - 1)) || B < 1 || S < 1 || !(sel >= 1.0) || !E_in || !A_out || !alpha || !beta || !G)
         return OPTIFAX_ERR_INVALID_ARGUMENT;
-    int time_mode, abc_mode, guard;
+    int time_mode, abc_mode, guard, nee = 0;
     switch (variant) {
         case OPTIFAX_VARIANT_BATCH_XTAL:
         case OPTIFAX_VARIANT_BATCH_OP: time_mode = 0; abc_mode = 0; guard = 1; break;
         case OPTIFAX_VARIANT_NO_BC: time_mode = 1; abc_mode = 1; guard = 0; break;
         case OPTIFAX_VARIANT_HARD_BC: time_mode = 1; abc_mode = 2; guard = 0; break;
+        case OPTIFAX_VARIANT_NEE: time_mode = 2; abc_mode = 3; guard = 0; nee = 1; break;
         default: return OPTIFAX_ERR_INVALID_ARGUMENT;
     }
     int dev = 0;
@@ -241,36 +261,38 @@ extern "C" int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_
     const int gstride = g_per_pulse ? S : 0;
     int nchunks = (int)((double)S / sel);
     if (guard && (double)nchunks * sel < (double)S) nchunks += 1;
-    double k = 0.0, stepprev = 4.0, stepmod = 4.0;
+    double k = nee ? 1.0 : 0.0, stepprev = 4.0, stepmod = 4.0;   // NEE_CPU.m: k is 1-based
     long long q = 0;
     int attempt = 0, acc = 0, rej = 0, status = 0;
     const long long max_attempts = 64LL * (S + 16) + 64;
     for (int chunk = 0; chunk < nchunks; ++chunk) {
-        stepmod = stepprev;
+        if (!nee) stepmod = stepprev;
         const double cend = (double)(chunk + 1) * sel;
-        while (k < cend && (!guard || k < (double)S)) {
+        while (k < cend && (nee ? k <= (double)S : (!guard || k < (double)S))) {
             if (attempt >= max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; goto done; }
-            const int kidx = k < 0.0 ? 0 : ((int)k >= S ? S - 1 : (int)k);
+            const double kg = nee ? k - 1.0 : k;     // G33(k) and the z of stage 1 are 1-based in NEE_CPU.m
+            const int kidx = kg < 0.0 ? 0 : ((int)kg >= S ? S - 1 : (int)kg);
             const int krec = (int)k;
             const double hmod = stepmod * step_h;
             cudaMemsetAsync(w.flags, 0, sizeof(int), st);
-            f64_nl<<<grid, 256, 0, st>>>(w.A0, w.NL, n, w0, dt, bdiffw0 * k * step_h, time_mode);
+            f64_nl<<<grid, 256, 0, st>>>(w.A0, w.NL, n, w0, dt, bdiffw0 * kg * step_h, time_mode);
             f64_k<<<grid, 256, 0, st>>>(w.NL, w.A0, w.K1, w.A1, G, gstride, kidx, hmod, cs, n, 0, max_err, min_err,
-                                        w.flags);
-            f64_nl<<<grid, 256, 0, st>>>(w.A1, w.NL, n, w0, dt, bdiffw0 * (k + stepmod) * step_h, time_mode);
+                                        nee, w.flags);
+            f64_nl<<<grid, 256, 0, st>>>(w.A1, w.NL, n, w0, dt, bdiffw0 * (kg + stepmod) * step_h, time_mode);
             f64_k<<<grid, 256, 0, st>>>(w.NL, w.A0, w.K1, w.A1, G, gstride, kidx, hmod, cs, n, 1, max_err, min_err,
-                                        w.flags);
+                                        nee, w.flags);
             cudaMemcpyAsync(w.hflags, w.flags, sizeof(int), cudaMemcpyDeviceToHost, st);
             if (cudaStreamSynchronize(st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
             const int fl = *w.hflags;
             if (fl & 4) status |= OPTIFAX_PULSE_NAN;
-            if ((fl & 1) && stepmod > 1.0 && (k - stepmod) > 0.0) {
+            bool accepted = false;
+            if ((fl & 1) && stepmod > 1.0 && (nee || (k - stepmod) > 0.0)) {
                 if (trace_host && attempt < trace_cap) {
                     trace_host[3 * attempt] = krec; trace_host[3 * attempt + 1] = (int)stepmod;
                     trace_host[3 * attempt + 2] = fl & 7;
                 }
                 ++rej;
-                k = k - stepmod;
+                if (!nee) k = k - stepmod;
                 stepmod = stepmod - 1.0;
                 stepprev = stepmod;
             } else {
@@ -279,14 +301,18 @@ extern "C" int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_
                     trace_host[3 * attempt + 2] = (fl & 7) | 8;
                 }
                 ++acc;
+                accepted = true;
                 const int s_used = (int)stepmod;
-                f64_abc<<<grid, 256, 0, st>>>(w.A1, n, abc_mode);
+                f64_abc<<<grid, 256, 0, st>>>(w.A1, n, abc_mode, dt);
                 fft64(w.A1, w.T, w.tw, n, B, +1, st);
                 f64_disp<<<grid, 256, 0, st>>>(w.T, alpha, beta, n, s_used);
                 fft64(w.T, w.A1, w.tw, n, B, -1, st);
                 f64_scale<<<grid, 256, 0, st>>>(w.A1, w.A0, n, 1.0 / (double)n);
                 q += s_used;
-                if (k + stepmod >= cend && k < cend - 1.0) {
+                if (nee) {    // NEE_CPU.m:77-83
+                    if (!(fl & 2)) stepmod = stepmod + 1.0;
+                    if (k < (double)S && k + stepmod > (double)S) stepmod = (double)S - k;
+                } else if (k + stepmod >= cend && k < cend - 1.0) {
                     double stepend = (cend - k) - 1.0;
                     stepprev = stepmod;
                     stepmod = stepend;
@@ -296,7 +322,7 @@ extern "C" int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_
                 }
             }
             ++attempt;
-            k = k + stepmod;
+            if (!nee || accepted) k = k + stepmod;
         }
     }
 done:

@@ -35,8 +35,8 @@ namespace cg = cooperative_groups;
 
 namespace ofx {
 
-enum { TIME_SHIFTED = 0, TIME_UNSHIFTED = 1 };
-enum { ABC_SOFT = 0, ABC_NONE = 1, ABC_HARD = 2 };
+enum { TIME_SHIFTED = 0, TIME_UNSHIFTED = 1, TIME_NEE = 2 };
+enum { ABC_SOFT = 0, ABC_NONE = 1, ABC_HARD = 2, ABC_NEE = 3 };
 
 struct PulseDev {
     const float2* E_in;
@@ -79,6 +79,7 @@ struct KernelCfg {
     int shared_sched;    // 1: OR the error flags over every pulse of the launch (grid barrier)
     int max_attempts_mul;
     int* grid_flags;     // 3 ints (shared schedule only)
+    int nee;             // NEE_CPU.m step control (Heun only)
 };
 
 // ---------------------------------------------------------------------------
@@ -103,11 +104,21 @@ __device__ __forceinline__ float2 k_eval(float2 nlm, float2 nl0, float2 nlp, flo
 
 __device__ __forceinline__ int time_index(int i, int n, int mode) {
     if (mode == TIME_SHIFTED) return (i > n / 2) ? i - n / 2 : i + n / 2;
+    if (mode == TIME_NEE) return (i < n / 2) ? i : i - n;      // fftshift(t), NEE_CPU.m:12,53
     return i;
 }
 
 __device__ __forceinline__ float abc_factor(int i, int n, int mode) {
     if (mode == ABC_NONE) return 1.f;
+    if (mode == ABC_NEE) {
+        // NEE_CPU.m:114-121: 1 - sech^2(24 (1 - |2t| / range(t))) where
+        // range(t) - |2t| < range(t) / 4, range(t) = (n - 1) dt, t = fftshift(t)
+        const int it = (i < n / 2) ? i : i - n;
+        const float r = 1.f - 2.f * fabsf((float)it) / (float)(n - 1);
+        if (!(r < 0.25f)) return 1.f;
+        const float th = tanhf(24.f * r);
+        return th * th;
+    }
     int gi1 = 6 * (n / 16), gi2 = 10 * (n / 16);
     if (!(i > gi1 && i < gi2)) return 1.f;
     if (mode == ABC_HARD) return 0.f;
@@ -130,6 +141,19 @@ __device__ __forceinline__ int classify(float scale, float2 d, float2 e, float m
         if (maxE <= 0.f || lhs >= hi * hi) bits = 1;
         else if (minE <= 0.f || lhs >= lo * lo) bits = 2;
     }
+    if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
+    return bits;
+}
+
+// NEE_CPU.m:73-79 class: pct = scale |d| / (|e| + 1) over every point; bit 0
+// when pct > maxErr (strict), bit 1 when pct >= minErr.
+__device__ __forceinline__ int classify_nee(float scale, float2 d, float2 e, float maxE, float minE) {
+    const float den = sqrtf(e.x * e.x + e.y * e.y) + 1.f;
+    const float lhs = scale * scale * (d.x * d.x + d.y * d.y);
+    const float hi = maxE * den, lo = minE * den;
+    int bits = 0;
+    if (lhs > hi * hi) bits |= 1;
+    if (lhs >= lo * lo) bits |= 2;
     if (!(isfinite(e.x) && isfinite(e.y))) bits |= 4;
     return bits;
 }
@@ -447,7 +471,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
     const int n_trips = P.n_trips > 0 ? P.n_trips : 1;
     const bool rec = (c == 0 && t == 0);
 
-    float k = 0.f, stepprev = 4.f, stepmod = 4.f;
+    const bool nee = cfg.nee != 0;           // NEE_CPU.m: k is 1-based, no chunk clamp
+    float k = nee ? 1.f : 0.f, stepprev = 4.f, stepmod = 4.f;
     unsigned q = 0;                          // accumulated dispersion position (sum of stepmod)
     int s_cached = -1;                       // stepmod of the cached per-mode D - 1 (Heun)
     int attempt = 0, n_acc = 0, n_rej = 0, status = 0, par = 0, trip = 0, trips_done = 0;
@@ -456,7 +481,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
 
     float2 k1r[16];   // RK23: K1 (first stage, FSAL) between attempts
     for (trip = 0; trip < n_trips; ++trip) {
-        k = 0.f; stepprev = 4.f; stepmod = 4.f; q = 0;
+        k = nee ? 1.f : 0.f; stepprev = 4.f; stepmod = 4.f; q = 0;
         attempt = 0; n_acc = 0; n_rej = 0;
         int trip_status = 0;
         double tally[4] = {0.0, 0.0, 0.0, 0.0};
@@ -477,18 +502,21 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
         }
 
         for (int chunk = 0; chunk < nchunks; ++chunk) {
-            stepmod = stepprev;
+            if (!nee) stepmod = stepprev;
             const float cend = (float)(chunk + 1) * sel;
-            while (k < cend && (!guard || k < Sf)) {
+            while (k < cend && (nee ? k <= Sf : (!guard || k < Sf))) {
                 if (attempt >= max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; goto done; }
-                const int kidx = (int)k;
+                const int kidx = nee ? (int)k - 1 : (int)k;   // G33(k) is 1-based in NEE_CPU.m
+                const int krec = (int)k;
+                const float kpos = nee ? k - 1.f : k;          // z of the first stage, in steps
+                bool accepted = false;
                 const float hmod = stepmod * h;
                 const float hg = hmod * G[kidx];
                 int bits = 0;
                 if constexpr (METHOD == OPTIFAX_HEUN) {
                     // ---- stage 1: K1 = f(A0) at z = k ----
                     float2 nl[16], k1[16], L, R;
-                    float2 z = zphase(P.tau_z4, k);
+                    float2 z = zphase(P.tau_z4, kpos);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) nl[j] = nl_eval(a[j], cph[j], z);
                     exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
@@ -496,7 +524,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     for (int j = 0; j < 16; ++j)
                         k1[j] = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
                     // ---- stage 2: K2 = f(A0 + K1) at z = k + stepmod ----
-                    z = zphase(P.tau_z4, k + stepmod);
+                    z = zphase(P.tau_z4, kpos + stepmod);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) nl[j] = nl_eval(cadd(a[j], k1[j]), cph[j], z);
                     exchange_edges<M, C>(edge, par, t, c, nl[0], nl[15], L, R);
@@ -504,9 +532,11 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         float2 k2 = k_eval(j == 0 ? L : nl[j - 1], nl[j], j == 15 ? R : nl[j + 1], hg, cs);
-                        float2 e = cadd(a[j], cadd(cscale(k2, 0.5f), cscale(k1[j], 0.5f)));
+                        // E = A0 + (K2/2 + K1/2) (MEX) or (A0 + K1/2) + K2/2 (NEE_CPU.m:75)
+                        float2 e = nee ? cadd(cadd(a[j], cscale(k1[j], 0.5f)), cscale(k2, 0.5f))
+                                       : cadd(a[j], cadd(cscale(k2, 0.5f), cscale(k1[j], 0.5f)));
                         float2 d = csub(k2, k1[j]);                        // = 2 (E - A1)
-                        bits |= classify(50.f, d, e, maxE, minE);
+                        bits |= nee ? classify_nee(50.f, d, e, maxE, minE) : classify(50.f, d, e, maxE, minE);
                         float2 ea = cscale(e, abc_s[j * T + t]);
                         bufE[phys(16 * t + j)] = ea;
                         if constexpr (C == 1) bufX[phys(16 * t + j)] = ea;
@@ -558,14 +588,15 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                 if (P.forced && gatt < P.n_forced) fl = (P.forced[gatt] & 3) | (fl & 4);
                 if (fl & 4) trip_status |= OPTIFAX_PULSE_NAN;
 
-                if ((fl & 1) && stepmod > 1.f && (k - stepmod) > 0.f) {
-                    // ---- reject: A0 unchanged; k moves back by one in net (the loop adds the new stepmod)
+                if ((fl & 1) && stepmod > 1.f && (nee || (k - stepmod) > 0.f)) {
+                    // ---- reject: A0 unchanged; MEX: k moves back by one in net (the loop
+                    // adds the new stepmod); NEE: k stays (NEE_CPU.m:68-70)
                     if (rec && P.trace && gatt < P.trace_cap) {
-                        P.trace[3 * gatt] = kidx; P.trace[3 * gatt + 1] = (int)stepmod;
+                        P.trace[3 * gatt] = krec; P.trace[3 * gatt + 1] = (int)stepmod;
                         P.trace[3 * gatt + 2] = fl & 7;
                     }
                     ++n_rej;
-                    k = k - stepmod;
+                    if (!nee) k = k - stepmod;
                     stepmod = stepmod - 1.f;
                     stepprev = stepmod;
                     if constexpr (METHOD == OPTIFAX_RK23) {
@@ -583,14 +614,20 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                 } else {
                     // ---- accept ----
                     if (rec && P.trace && gatt < P.trace_cap) {
-                        P.trace[3 * gatt] = kidx; P.trace[3 * gatt + 1] = (int)stepmod;
+                        P.trace[3 * gatt] = krec; P.trace[3 * gatt + 1] = (int)stepmod;
                         P.trace[3 * gatt + 2] = (fl & 7) | 8;
                     }
                     ++n_acc;
+                    accepted = true;
                     const int s_used = (int)stepmod;
-                    if (rec && P.stepmods && kidx < P.stepmods_limit && kidx < P.S) P.stepmods[kidx] = (float)s_used;
-                    // step control (OPO_CUDA_BATCH_XTAL.cu:487-506; ODE23 :519-538 doubles)
-                    if (k + stepmod >= cend && k < cend - 1.f) {
+                    if (!nee && rec && P.stepmods && kidx < P.stepmods_limit && kidx < P.S)
+                        P.stepmods[kidx] = (float)s_used;
+                    // step control (OPO_CUDA_BATCH_XTAL.cu:487-506; ODE23 :519-538 doubles;
+                    // NEE_CPU.m:77-83: grow below minErr, clamp only at the crystal end)
+                    if (nee) {
+                        if (!(fl & 2)) stepmod = stepmod + 1.f;
+                        if (k < Sf && k + stepmod > Sf) stepmod = Sf - k;
+                    } else if (k + stepmod >= cend && k < cend - 1.f) {
                         float stepend = (cend - k) - 1.f;
                         stepprev = stepmod;
                         stepmod = stepend;
@@ -603,8 +640,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                         stepprev = stepmod;
                     }
                     const float knext = k + stepmod;
-                    const bool last_in_chunk = !(knext < cend && (!guard || knext < Sf));
-                    const bool pass_ends = !(knext < pass_end && (!guard || knext < Sf));
+                    const bool last_in_chunk = !(knext < cend && (nee ? knext <= Sf : (!guard || knext < Sf)));
+                    const bool pass_ends = !(knext < pass_end && (nee ? knext <= Sf : (!guard || knext < Sf)));
                     const bool cav = opo && pass_ends;
                     const unsigned qn = q + (unsigned)s_used;
 
@@ -709,7 +746,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                 }
                 ++attempt;
                 ++gatt;
-                k = k + stepmod;
+                if (!nee || accepted) k = k + stepmod;
             }
         }
         status |= trip_status;

@@ -21,7 +21,7 @@ import torch
 
 from . import _native as nat
 from ._native import (HEUN, RK23, VARIANT_BATCH_XTAL, VARIANT_BATCH_OP, VARIANT_NO_BC,
-                      VARIANT_HARD_BC, VARIANT_ODE23, Context, check)
+                      VARIANT_HARD_BC, VARIANT_ODE23, VARIANT_NEE, Context, check)
 
 _contexts = {}
 

@@ -31,6 +31,11 @@ def _fp64_gpu(si, E, variant, trace_cap=200000, G=None):
 
 
 def _oracle(oracle, si, E, variant, G=None, shared=False):
+    if variant == 5:
+        return oracle.run(E, si.alpha, si.G if G is None else G, si.beta, w0=si.w0, bdiffw0=si.bdiffw0,
+                          h=si.h, n_steps=si.n_steps, dt=si.dt, max_err=si.max_err, min_err=si.min_err,
+                          sel=si.sel, method=oracle.HEUN_NEE, g_per_pulse=G is not None,
+                          shared_schedule=shared, trace_cap=200000)
     tm, abc, ch = {0: (oracle.TIME_SHIFTED, oracle.ABC_SOFT, oracle.CHUNKS_CEIL),
                    1: (oracle.TIME_SHIFTED, oracle.ABC_SOFT, oracle.CHUNKS_CEIL),
                    2: (oracle.TIME_UNSHIFTED, oracle.ABC_NONE, oracle.CHUNKS_TRUNC),
@@ -41,7 +46,7 @@ def _oracle(oracle, si, E, variant, G=None, shared=False):
                       g_per_pulse=G is not None, shared_schedule=shared, trace_cap=200000)
 
 
-@pytest.mark.parametrize("N,variant", [(1024, 0), (2048, 0), (1024, 2), (2048, 3), (512, 1)])
+@pytest.mark.parametrize("N,variant", [(1024, 0), (2048, 0), (1024, 2), (2048, 3), (512, 1), (1024, 5), (2048, 5)])
 def test_fp64_single_pulse(oracle, N, variant):
     win, si, E = make_case(N=N, length=0.2e-3, power=2.0)
     A, st, tr = _fp64_gpu(si, E[0], variant)

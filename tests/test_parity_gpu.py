@@ -48,6 +48,10 @@ def _oracle_pass(oracle, si, E, method, variant, forced=None):
             nat.VARIANT_NO_BC: (oracle.TIME_UNSHIFTED, oracle.ABC_NONE, oracle.CHUNKS_TRUNC, 128),
             nat.VARIANT_HARD_BC: (oracle.TIME_UNSHIFTED, oracle.ABC_HARD, oracle.CHUNKS_TRUNC, 128),
             nat.VARIANT_ODE23: (oracle.TIME_UNSHIFTED, oracle.ABC_SOFT, oracle.CHUNKS_TRUNC, 256)}
+    if variant == nat.VARIANT_NEE:
+        return oracle.run(E, si.alpha, si.G, si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                          n_steps=si.n_steps, dt=si.dt, max_err=si.max_err, min_err=si.min_err,
+                          sel=si.sel, method=oracle.HEUN_NEE, trace_cap=200000, forced=forced)
     tm, abc, ch, rule = vmap[variant]
     N = E.shape[-1]
     lim = -(-N // 128) * 128 if rule == 128 else (N // 256) * 256
@@ -105,6 +109,23 @@ def test_rk23_ode23(oracle, N, cta):
     from optifax_gb300 import _native as nat
     win, si, E = make_case(N=N, length=0.2e-3, power=2.0)
     check_parity(oracle, si, E[0], nat.RK23, nat.VARIANT_ODE23, cta)
+
+
+@pytest.mark.parametrize("N,cta", [(1024, 0), (4096, 0), (8192, 4096)])
+def test_nee_variant(oracle, N, cta):
+    """NEE_CPU.m semantics on the GPU kernel (k 1-based, reject keeps k, growth
+    below minErr, clamp only at the crystal end, t-based absorber, fftshift(t))."""
+    from optifax_gb300 import _native as nat
+    win, si, E = make_case(N=N, length=0.2e-3, power=2.0)
+    info = check_parity(oracle, si, E[0], nat.HEUN, nat.VARIANT_NEE, cta)
+    print(info)
+
+
+def test_nee_rejects_rk23():
+    from optifax_gb300 import _native as nat
+    win, si, E = make_case(N=1024, length=0.1e-3)
+    with pytest.raises(nat.OptifaxError):
+        _gpu_pass(si, E[0], nat.RK23, nat.VARIANT_NEE)
 
 
 def test_heun_tight_tolerance(oracle):
