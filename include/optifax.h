@@ -132,6 +132,12 @@ typedef struct {
     float steady_tol;            /* |T_n - T_{n-1}| <= tol |T_n| counts as flat */
     int32_t reserved;
     void* history;               /* optional: n_trips x N complex, crystal-output spectrum X of each trip */
+    const float* esd_w;          /* optional: n_esd x N weights (OpticalSim.averageSimPulses, OpticalSim.m:303-315) */
+    float* esd;                  /* n_esd x N accumulators: esd[i][k] += esd_w[i][k] |X_k|^2 every trip */
+    int32_t n_esd;               /* 0..4 */
+    int32_t reserved2;
+    float* stepmods_trips;       /* optional: n_trips x n_steps, each trip's stepmods record
+                                    (StepSizeModifiers, OpticalSim.m:172,237-252) */
 } optifax_opo;
 
 /* Create / destroy a context on a CUDA device.  The context owns the twiddle

@@ -483,6 +483,12 @@ int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cav
         d.steady_tally = cv.steady_tally;
         d.steady_tol = cv.steady_tol;
         d.hist = (float2*)cv.history;
+        if (cv.n_esd < 0 || cv.n_esd > 4 || (cv.n_esd > 0 && (!cv.esd_w || !cv.esd)))
+            return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_esd must be 0..4 with esd_w and esd");
+        d.esd_w = cv.n_esd > 0 ? cv.esd_w : nullptr;
+        d.esd = cv.n_esd > 0 ? cv.esd : nullptr;
+        d.n_esd = cv.n_esd;
+        d.smt = cv.stepmods_trips;
         int M = choose_M(cv.pass.n_points, cta_points);
         if (M > cv.pass.n_points) M = cv.pass.n_points;
         int C = cv.pass.n_points / M;

@@ -62,6 +62,10 @@ struct PulseDev {
     int n_trips, n_tally, steady_trips, steady_tally;
     float steady_tol;
     float2* hist;            // optional per-trip crystal-output spectra (n_trips x N)
+    const float* esd_w;      // n_esd x N spectral-energy weights (trip sums into esd)
+    float* esd;
+    int n_esd;
+    float* smt;              // optional per-trip stepmods records (n_trips x S)
     // cluster (C > 1) exchange scratch in global memory: 2 N complex
     float2* xch;
 };
@@ -622,6 +626,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     const int s_used = (int)stepmod;
                     if (!nee && rec && P.stepmods && kidx < P.stepmods_limit && kidx < P.S)
                         P.stepmods[kidx] = (float)s_used;
+                    if (!nee && rec && P.smt && kidx < P.stepmods_limit && kidx < P.S)
+                        P.smt[(size_t)trip * P.S + kidx] = (float)s_used;
                     // step control (OPO_CUDA_BATCH_XTAL.cu:487-506; ODE23 :519-538 doubles;
                     // NEE_CPU.m:77-83: grow below minErr, clamp only at the crystal end)
                     if (nee) {
@@ -708,6 +714,12 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                             for (int i = 0; i < 4; ++i)
                                 if (i < P.n_tally) part[i] = fmaf(P.tally_w[(size_t)i * N + kk], x2, part[i]);
                             if (P.hist) P.hist[(size_t)trip * N + kk] = X;
+                            if (P.esd) {
+                                // every mode has one owner thread: plain read-modify-write
+#pragma unroll
+                                for (int i = 0; i < 4; ++i)
+                                    if (i < P.n_esd) P.esd[(size_t)i * N + kk] += P.esd_w[(size_t)i * N + kk] * x2;
+                            }
                             v[j] = cadd(cmul(X, P.fb[kk]), P.pump[kk]);
                         } else {
                             v[j] = cmul(eh, dm1);

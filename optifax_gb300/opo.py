@@ -27,6 +27,7 @@ from . import physics as ph
 from .solver import context, _stream_ptr
 
 TALLY_OUTPUT, TALLY_OUTPUT_SIGNAL, TALLY_INTRACAVITY, TALLY_PUMP_BAND = range(4)
+ESD_OUTPUT, ESD_XTAL_OUT = range(2)
 
 
 class OptifaxOpo(ctypes.Structure):
@@ -34,7 +35,9 @@ class OptifaxOpo(ctypes.Structure):
                 ("tally_w", ctypes.c_void_p), ("trips", ctypes.c_void_p),
                 ("n_trips", ctypes.c_int32), ("n_tally", ctypes.c_int32),
                 ("steady_trips", ctypes.c_int32), ("steady_tally", ctypes.c_int32),
-                ("steady_tol", ctypes.c_float), ("reserved", ctypes.c_int32), ("history", ctypes.c_void_p)]
+                ("steady_tol", ctypes.c_float), ("reserved", ctypes.c_int32), ("history", ctypes.c_void_p),
+                ("esd_w", ctypes.c_void_p), ("esd", ctypes.c_void_p), ("n_esd", ctypes.c_int32),
+                ("reserved2", ctypes.c_int32), ("stepmods_trips", ctypes.c_void_p)]
 
 
 TRIP_RECORD_BYTES = 48
@@ -72,6 +75,7 @@ class CavityArrays:
     pump: np.ndarray          # natural FFT order, complex128
     tally_w: np.ndarray       # (4, N) float64
     unit: float               # J per |X|^2 in air
+    esd_w: np.ndarray = None  # (2, N): pJ/THz per |X|^2 of the output-coupled and crystal-output pulses
 
 
 def build_cavity(spec: CavitySpec) -> CavityArrays:
@@ -102,7 +106,11 @@ def build_cavity(spec: CavitySpec) -> CavityArrays:
                         unit * r_out2 * t_filter * spec.oc_output * sig,
                         unit * r_out2,
                         unit * r_out2 * pband])
-    return CavityArrays(win=win, si=si, E0=E0, feedback=feedback, pump=pump_k, tally_w=tally_w, unit=unit)
+    # energy spectral densities in pJ/THz (OpticalPulse.ESD_pJ_THz: I2pow / dNu * 1e24)
+    df = 1.0 / (n * win.dt)
+    esd_w = np.stack([tally_w[0], tally_w[2]]) / df * 1e24
+    return CavityArrays(win=win, si=si, E0=E0, feedback=feedback, pump=pump_k, tally_w=tally_w, unit=unit,
+                        esd_w=esd_w)
 
 
 @dataclasses.dataclass
@@ -114,6 +122,8 @@ class OpoResult:
     trips_dev: Optional[torch.Tensor] = None
     stats_dev: Optional[torch.Tensor] = None
     history: Optional[torch.Tensor] = None   # (n_trips, N) crystal-output spectra when requested
+    esd: Optional[torch.Tensor] = None       # (2, N) trip sums of the ESDs (pJ/THz), natural FFT order
+    step_size_modifiers: Optional[torch.Tensor] = None   # (n_trips, S) per-trip stepmods records
 
     def decode(self):
         """Copy the device records to the host (after the stream has finished)."""
@@ -145,13 +155,14 @@ class OpticalSim:
         self.feedback = t(a.feedback, np.complex64)
         self.pump = t(a.pump, np.complex64)
         self.tally_w = t(a.tally_w, np.float32)
+        self.esd_w = t(a.esd_w, np.float32)
         self.field = t(a.E0, np.complex64)
         self.variant = variant
         self.cta_points = cta_points
         self.ctx = context(device)
         self.trip_number = 0
 
-    def _descriptor(self, n_trips, steady_tol, steady_trips, steady_tally, history):
+    def _descriptor(self, n_trips, steady_tol, steady_trips, steady_tally, history, esd=False, steps=False):
         si = self.arrays.si
         N = self.field.numel()
         out = torch.empty_like(self.field)
@@ -169,20 +180,46 @@ class OpticalSim:
         cv.steady_trips, cv.steady_tally, cv.steady_tol = int(steady_trips), int(steady_tally), float(steady_tol)
         hist = torch.zeros((n_trips, N), dtype=torch.complex64, device=self.dev) if history else None
         cv.history = hist.data_ptr() if hist is not None else None
-        return cv, out, trips, hist
+        esd_acc = torch.zeros((2, N), dtype=torch.float32, device=self.dev) if esd else None
+        if esd_acc is not None:
+            cv.esd_w, cv.esd, cv.n_esd = self.esd_w.data_ptr(), esd_acc.data_ptr(), 2
+        smt = torch.zeros((n_trips, si.n_steps), dtype=torch.float32, device=self.dev) if steps else None
+        cv.stepmods_trips = smt.data_ptr() if smt is not None else None
+        return cv, out, trips, hist, esd_acc, smt
 
     def run(self, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
             steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
-            history: bool = False) -> OpoResult:
+            history: bool = False, esd: bool = False, step_records: bool = False) -> OpoResult:
         """Run n_trips round trips in one launch.  history=True also returns every
-        trip's crystal-output spectrum X (n_trips, N) in ``result.history``."""
+        trip's crystal-output spectrum X (n_trips, N) in ``result.history``; esd=True
+        the trip sums of the output-coupled and crystal-output ESDs (``result.esd``,
+        see ``esd_averages``); step_records=True each trip's stepmods record
+        (``result.step_size_modifiers``, OpticalSim.StepSizeModifiers)."""
         return run_many([self], n_trips, steady_tol=steady_tol, steady_trips=steady_trips,
-                        steady_tally=steady_tally, stream=stream, host_out=host_out, history=history)[0]
+                        steady_tally=steady_tally, stream=stream, host_out=host_out, history=history,
+                        esd=esd, step_records=step_records)[0]
+
+    def esd_averages(self, res: OpoResult) -> dict:
+        """OpticalSim.averageSimPulses (OpticalSim.m:303-315) from a run's ESD sums:
+        the output ESD averaged over the trips, the crystal-output ESD below the pump
+        limit (lambda_pump + 5 linewidths, "pump depletion") and above twice that limit
+        ("idler"), all in pJ/THz per FFT bin, with the wavelengths (natural FFT order)."""
+        if res.esd is None:
+            raise ValueError("run with esd=True")
+        n = max(res.trips_done, 1)
+        e = res.esd.double().cpu().numpy() / n
+        lam_nm = np.fft.ifftshift(self.arrays.win.wavelengths) * 1e9
+        lw = ph.default_linewidth(self.spec.pump_wavelength, self.spec.pump_tau)
+        pump_lim = (self.spec.pump_wavelength + 5 * lw) * 1e9
+        xt = e[ESD_XTAL_OUT]
+        return {"wavelength_nm": lam_nm, "out": e[ESD_OUTPUT],
+                "pump_depletion": np.where(lam_nm > pump_lim, 0.0, xt),
+                "idler": np.where(lam_nm < 2 * pump_lim, 0.0, xt)}
 
 
 def run_many(sims, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
              steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
-             history: bool = False):
+             history: bool = False, esd: bool = False, step_records: bool = False):
     """Run several independent cavities (same device) for n_trips each in one launch."""
     if not sims:
         raise ValueError("no cavities")
@@ -192,9 +229,10 @@ def run_many(sims, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int =
     for i, sim in enumerate(sims):
         if sim.dev != dev or sim.variant != sims[0].variant:
             raise ValueError("cavities of one launch share the device and the variant")
-        cv, out, trips, hist = sim._descriptor(n_trips, steady_tol, steady_trips, steady_tally, history)
+        cv, out, trips, hist, esd_acc, smt = sim._descriptor(n_trips, steady_tol, steady_trips, steady_tally,
+                                                             history, esd, step_records)
         arr[i] = cv
-        outs.append((out, trips, hist))
+        outs.append((out, trips, hist, esd_acc, smt))
     stats = torch.zeros((len(sims), nat.STATS_BYTES // 4), dtype=torch.int32, device=dev)
     ctx = sims[0].ctx
     lib = ctx.lib
@@ -204,11 +242,13 @@ def run_many(sims, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int =
                              stats.data_ptr(), _stream_ptr(stream))
     nat.check(rc, ctx.handle, "optifax_opo_run")
     results = []
-    for i, (sim, (out, trips, hist)) in enumerate(zip(sims, outs)):
+    for i, (sim, (out, trips, hist, esd_acc, smt)) in enumerate(zip(sims, outs)):
         sim.field = out
         res = OpoResult(field=out, trips=None, trips_done=-1, stats={}, trips_dev=trips,
                         stats_dev=stats[i:i + 1])
         res.history = hist
+        res.esd = esd_acc
+        res.step_size_modifiers = smt
         if host_out:
             res.trips, res.trips_done, res.stats = res.decode()
             sim.trip_number += res.trips_done

@@ -81,3 +81,29 @@ def test_opo_steady_state_stop():
     res = sim.run(50, steady_tol=0.5, steady_trips=3, steady_tally=opo.TALLY_INTRACAVITY)
     assert 3 < res.trips_done < 50
     assert np.all(res.trips["status"] == 0)
+
+
+def test_opo_diagnostics_esd_and_step_records():
+    """ESD trip sums and per-trip stepmods records (OpticalSim.averageSimPulses and
+    StepSizeModifiers) against the recorded per-trip crystal outputs."""
+    from optifax_gb300 import opo
+    spec = opo.CavitySpec(n_points=2048, window=2048 * 6e-12 / 2 ** 13, crystal_length=0.2e-3,
+                          pump_tau=100e-15, pump_power=1.5, seed=3)
+    sim = opo.OpticalSim(spec)
+    res = sim.run(3, history=True, esd=True, step_records=True)
+    X = res.history.cpu().numpy().astype(np.complex128)
+    w = sim.arrays.esd_w
+    ref = np.stack([np.sum(w[i] * np.abs(X) ** 2, axis=0) for i in range(2)])
+    got = res.esd.cpu().numpy()
+    for i in range(2):
+        assert np.abs(got[i] - ref[i]).max() <= 1e-5 * ref[i].max()
+    av = sim.esd_averages(res)
+    assert np.allclose(av["out"], got[0] / 3, rtol=1e-6, atol=0)
+    assert np.all(av["pump_depletion"][av["wavelength_nm"] > 1100] == 0)
+    smt = res.step_size_modifiers.cpu().numpy()
+    assert smt.shape == (3, sim.arrays.si.n_steps)
+    for r in range(3):
+        s_ = smt[r][smt[r] > 0]
+        assert np.all(s_ == np.round(s_)) and s_.max() <= 64
+        # one record per accepted step (accepted steps sit at strictly increasing k < S)
+        assert len(s_) == res.trips["accepted"][r]
