@@ -330,6 +330,39 @@ int optifax_ff_encode_env(const void* spectra, int64_t stride, int32_t n_spectra
 int optifax_ff_decode_env(const float* y, const float* sigma, int32_t n_points, int32_t n_bins,
                           const int32_t* band, float pump_scale, void* X_out, void* stream);
 
+/*
+ * Solver inputs computed on the device (OpticalSim.m:213-226 precompute) for many
+ * pulses at once: per pulse the dispersion phase per step (phi_calc.m:14-45, MgO:LN
+ * Sellmeier of Gayer et al., group delay at the reference removed), the per-step
+ * transmission, the QPM drive from the given domain walls (QPMcrystal.m:20-51) and
+ * the in-crystal input field (sech^2 pump, sechPulse.m / Laser.m:66-77, plus one
+ * photon per mode with a counter-based phase keyed by `seed`, refracted into the
+ * crystal).  Scalars (dt exactly as the host grid computes it, t_rms of the pump,
+ * g_scale = chi2 w0 / (n0 4 c)) come from the host.  Outputs alpha, beta (N floats),
+ * G (S floats) and E (N complex64) are DEVICE arrays in the solver's layout; walls
+ * (DEVICE, ascending, < length) give the domain boundaries.  work: DEVICE scratch of
+ * optifax_setup_work_bytes(max n_points) bytes, reused pulse by pulse.
+ */
+typedef struct {
+    int32_t n_points, n_steps;
+    double window, dt;                 /* temporal range and sample spacing [s] */
+    double lambda_ref;                 /* grid reference wavelength [m] */
+    double length, step_size, celsius; /* crystal length and solver step [m], temperature */
+    double g_scale;
+    const double* walls;
+    int32_t n_walls;
+    int32_t seed;
+    double pump_lambda, pump_t_rms, pump_energy, waist, n_medium;
+    double lambda_lo_nm, lambda_hi_nm; /* transmission window (inside 200-20000 nm) */
+    float* alpha;
+    float* beta;
+    float* G;
+    void* E;
+} optifax_setup;
+int64_t optifax_setup_work_bytes(int32_t max_points);
+int optifax_setup_pulses(const optifax_setup* s, int32_t n, void* work, int64_t work_bytes,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif

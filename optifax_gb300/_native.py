@@ -20,7 +20,7 @@ EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifa
            "optifax_fno_param_count", "optifax_fno_create", "optifax_fno_destroy", "optifax_fno_set_params",
            "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
            "optifax_ff_encode", "optifax_ff_step",
-           "optifax_ff_encode_env", "optifax_ff_decode_env"]
+           "optifax_ff_encode_env", "optifax_ff_decode_env", "optifax_setup_work_bytes", "optifax_setup_pulses"]
 
 _lib = None
 
@@ -112,8 +112,24 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_ff_encode_env.restype = ctypes.c_int
     lib.optifax_ff_decode_env.argtypes = [vp, vp, i32, i32, ctypes.POINTER(i32), f32, vp, vp]
     lib.optifax_ff_decode_env.restype = ctypes.c_int
+    lib.optifax_setup_work_bytes.argtypes = [i32]
+    lib.optifax_setup_work_bytes.restype = ctypes.c_int64
+    lib.optifax_setup_pulses.argtypes = [ctypes.POINTER(OptifaxSetup), i32, vp, i64, vp]
+    lib.optifax_setup_pulses.restype = ctypes.c_int
     _lib = lib
     return lib
+
+
+class OptifaxSetup(ctypes.Structure):
+    _fields_ = [("n_points", ctypes.c_int32), ("n_steps", ctypes.c_int32),
+                ("window", ctypes.c_double), ("dt", ctypes.c_double), ("lambda_ref", ctypes.c_double),
+                ("length", ctypes.c_double), ("step_size", ctypes.c_double), ("celsius", ctypes.c_double),
+                ("g_scale", ctypes.c_double), ("walls", ctypes.c_void_p), ("n_walls", ctypes.c_int32),
+                ("seed", ctypes.c_int32), ("pump_lambda", ctypes.c_double), ("pump_t_rms", ctypes.c_double),
+                ("pump_energy", ctypes.c_double), ("waist", ctypes.c_double), ("n_medium", ctypes.c_double),
+                ("lambda_lo_nm", ctypes.c_double), ("lambda_hi_nm", ctypes.c_double),
+                ("alpha", ctypes.c_void_p), ("beta", ctypes.c_void_p), ("G", ctypes.c_void_p),
+                ("E", ctypes.c_void_p)]
 
 
 class OptifaxError(RuntimeError):

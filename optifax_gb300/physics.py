@@ -164,6 +164,14 @@ def qpm_signs(n_steps: int, length: float, period) -> np.ndarray:
     the reference's discretised power-law chirp (chirped_domain_widths).
     """
     z = np.linspace(0.0, length, n_steps)
+    edges = np.concatenate([[0.0], qpm_walls(z, length, period)])
+    q = np.searchsorted(edges, z, side="right")      # 1-based domain index
+    q = np.mod(q, 2)
+    return -(2.0 * q - 1.0)
+
+
+def qpm_walls(z: np.ndarray, length: float, period) -> np.ndarray:
+    """Domain-wall positions (ascending, < length) of qpm_signs' gratings."""
     if isinstance(period, (tuple, list)) and period[0] == "chirpedgrating":
         widths = chirped_domain_widths(z, *period[1:])
         walls = np.cumsum(widths)
@@ -180,10 +188,7 @@ def qpm_signs(n_steps: int, length: float, period) -> np.ndarray:
         n_dom = int(np.floor(2.0 * length / p))
         walls = np.cumsum(np.full(n_dom, p / 2.0))
         walls = walls[walls < length]
-    edges = np.concatenate([[0.0], walls])
-    q = np.searchsorted(edges, z, side="right")      # 1-based domain index
-    q = np.mod(q, 2)
-    return -(2.0 * q - 1.0)
+    return walls
 
 
 def chirped_domain_widths(z: np.ndarray, p1: float, p2: float, a: float = 1.0,
@@ -272,6 +277,24 @@ class SolverInputs:
     n0: float
 
 
+def solver_scalars(xtal: Crystal, win: SimWindow) -> dict:
+    """The scalar solver inputs of OpticalSim.run (w0, bdiffw0, n0, the G33
+    magnitude) from the index at the reference bin and the one below it."""
+    r = win.ref_index
+    w = win.omegas[r - 1:r + 1]
+    lam = win.wavelengths[r - 1:r + 1]
+    n = n_mgoln_e(lam * 1e6, xtal.celsius)
+    phi_abs = xtal.length * (w * n / C0)
+    n0 = float(n[1])
+    w0 = float(np.float32(win.reference_omega))
+    beta0_w0 = float((2 * np.pi * n / lam)[1])
+    # xtal.GroupDelay = phi2GD(Bulk.Phi, dw) (Optic.m:130-133, phi2GD.m:1-15):
+    # backward first difference at the reference index, per unit length
+    beta1_w0 = float((phi_abs[1] - phi_abs[0]) / win.d_omega / xtal.length)
+    return {"n0": n0, "w0": w0, "bdiffw0": beta0_w0 - beta1_w0 * w0,
+            "g_scale": xtal.chi2 * w0 / n0 / 4.0 / C0}
+
+
 def solver_inputs(xtal: Crystal, win: SimWindow, error_bounds=(2.5e-3, 5e-2),
                   progress_plots: int = 5) -> SolverInputs:
     """OpticalSim.run precompute (OpticalSim.m:213-226)."""
@@ -279,18 +302,10 @@ def solver_inputs(xtal: Crystal, win: SimWindow, error_bounds=(2.5e-3, 5e-2),
     S = xtal.n_steps
     sel = float(math.ceil(S / (progress_plots - 1)))
     phi_rel, phi_abs, n = phi_calc(xtal.length, win, xtal.celsius)
-    r = win.ref_index
-    n0 = float(n[r])
-    w0 = f32(win.reference_omega)
+    sc = solver_scalars(xtal, win)
+    n0, w0, bdiffw0 = sc["n0"], sc["w0"], sc["bdiffw0"]
     P = qpm_signs(S, xtal.length, xtal.period)
     G = (P * xtal.chi2 * w0 / n0 / 4.0 / C0).astype(np.float32)
-    lam = win.wavelengths
-    beta0_abs = 2 * np.pi * n / lam
-    beta0_w0 = float(beta0_abs[r])
-    # xtal.GroupDelay = phi2GD(Bulk.Phi, dw) (Optic.m:130-133, phi2GD.m:1-15):
-    # backward first difference at the reference index, per unit length
-    beta1_w0 = float((phi_abs[r] - phi_abs[r - 1]) / win.d_omega / xtal.length)
-    bdiffw0 = beta0_w0 - beta1_w0 * w0
     T = window_transmission(win)
     with np.errstate(divide="ignore", invalid="ignore"):
         alpha = np.where(T > 0, T ** (1.0 / S), 0.0)
@@ -315,6 +330,15 @@ def default_linewidth(lambda_c: float, dtau: float) -> float:
     return (4 * C0 * 0.315 * dtau * lambda_c ** 2) / ((2 * C0 * dtau) ** 2 - (lambda_c * 0.315) ** 2)
 
 
+def sech_t_rms(lambda_c: float, dtau: float) -> float:
+    """sech width parameter of a transform-limited sech^2 of FWHM dtau (sechPulse.m)."""
+    dlam = default_linewidth(lambda_c, dtau)
+    edges = lambda_c + np.array([-dlam, dlam]) / 2.0
+    nu_fwhm = float(np.ptp(C0 / edges))
+    t_fwhm = 0.315 / nu_fwhm
+    return t_fwhm / (2 * np.log(1 + 2 ** 0.5))
+
+
 def sech_pump(win: SimWindow, lambda_c: float, dtau: float, avg_power: float,
               f_rep: float = 100e6, waist: float = 15e-6, n_medium: float = 1.0) -> np.ndarray:
     """sech^2 pump field [V/m] on the natural time grid (sechPulse.m, Laser.m:66-77).
@@ -326,11 +350,7 @@ def sech_pump(win: SimWindow, lambda_c: float, dtau: float, avg_power: float,
     temporal phase.
     """
     t = win.times
-    dlam = default_linewidth(lambda_c, dtau)
-    edges = lambda_c + np.array([-dlam, dlam]) / 2.0
-    nu_fwhm = float(np.ptp(C0 / edges))
-    t_fwhm = 0.315 / nu_fwhm
-    t_rms = t_fwhm / (2 * np.log(1 + 2 ** 0.5))
+    t_rms = sech_t_rms(lambda_c, dtau)
     u = 1.0 / np.cosh(t / t_rms)
     w_p = 2 * np.pi * C0 / lambda_c
     u = u * np.exp(1j * (w_p - win.reference_omega) * t)
