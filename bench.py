@@ -180,6 +180,35 @@ def pass_case(n_points: int, length: float, cta_points: int, reps: int = 2):
                           "attempts": st["attempts"], "ms": ms, "us_per_attempt": 1000 * ms / st["attempts"]}))
 
 
+def fno_case(batch: int, reps: int = 3):
+    """Profiling case: `reps` training steps (forward, backward, AdamW) of the
+    surrogate network on synthetic data, batch x 6 x 4096; prints per-step device
+    time and the tensor-core FLOPs of the step's GEMMs."""
+    import torch
+    from optifax_gb300.surrogate import FNO
+    from optifax_gb300.gemm import tc_error
+    L = 4096
+    net = FNO(n_bins=L, max_batch=batch, seed=1)
+    g = torch.Generator(device="cuda").manual_seed(1)
+    x = torch.randn((batch, 6, L), generator=g, device="cuda")
+    t = torch.randn((batch, 4, L), generator=g, device="cuda")
+    # GEMM FLOPs per step: forward 3 per layer, backward 4 per layer
+    W, SPEC = 64, 64
+    fwd = 2 * (W * batch * SPEC * L) + 2 * (W * batch * L * SPEC) + 2 * (batch * L * W * W)
+    bwd = 2 * (W * W * batch * L) + 2 * (W * batch * SPEC * L) + 2 * (W * batch * L * SPEC) + 2 * (batch * L * W * W)
+    flops = 4 * (fwd + bwd)
+    for _ in range(reps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        net.backward(x, t)
+        net.adam(1e-3)
+        ev1.record()
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        print(json.dumps({"case": "fno_train_step", "batch": batch, "ms": ms, "gemm_gflop": flops / 1e9,
+                          "gemm_tflops_over_step": flops / (ms / 1e3) / 1e12, "tc_error": tc_error()}))
+
+
 def run_sweep(args):
     """Config 3: a batch of crystal passes with uneven grids (2^12..2^16), crystals
     (0.5-10 mm, 28-32 um), pumps (0.5-3 W, 100-300 fs), seed 2, in one call.
@@ -244,9 +273,13 @@ def main():
     ap.add_argument("--sweep-size", type=int, default=256)
     ap.add_argument("--fp64-trips", type=int, default=1,
                     help="round trips of the plain FP64 solver timed beside the line (0: skip)")
+    ap.add_argument("--fno-case", type=int, default=0,
+                    help="profiling case: surrogate training steps at this batch size, no JSON bench line")
     ap.add_argument("--pass-case", default=None,
                     help="profiling case 'N,length_m': one crystal pass, run twice, no JSON bench line")
     args = ap.parse_args()
+    if args.fno_case:
+        return fno_case(args.fno_case)
     if args.pass_case:
         n, length = args.pass_case.split(",")
         return pass_case(int(n), float(length), args.cta_points)

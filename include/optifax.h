@@ -51,7 +51,8 @@ typedef enum {
     OPTIFAX_VARIANT_HARD_BC = 3,    /* unshifted time, hard absorber (OPO_CUDA_HARD_BC.cu:118-129) */
     OPTIFAX_VARIANT_ODE23 = 4,      /* unshifted time, sech^2 absorber, truncated chunks, shared G (OPO_CUDA_ODE23.cu) */
     OPTIFAX_VARIANT_NEE = 5         /* NEE_CPU.m:1-122 (Heun): fftshift(t), t-based absorber, 1-based G, reject keeps k,
-                                       grow below minErr, clamp only at the crystal end, snapshot fft(A) per chunk */
+                                       grow below minErr, clamp only at the crystal end, snapshot fft(A) per chunk;
+                                       grids up to 2^14 points */
 } optifax_variant;
 
 /* Per-pulse status bits returned in optifax_pulse_stats.status. */

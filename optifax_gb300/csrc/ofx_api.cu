@@ -119,6 +119,7 @@ const std::vector<KernelEntry>& kernel_table() {
         register_kernels_heun_large(v);
         register_kernels_heun_small(v);
         register_kernels_rk23(v);
+        register_kernels_heun_nee(v);
         return v;
     }();
     return tbl;
@@ -199,6 +200,8 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
                          [](const PulseDev& x, const PulseDev& y) { return pulse_cost(x) > pulse_cost(y); });
         n_desc += g.d.size();
         if (g.C > 1) need_xch += g.d.size() * 2 * (size_t)g.M * g.C;
+        for (const auto& d : g.d)
+            if (d.esd && !d.hist) need_xch += (size_t)g.M * g.C;    // trip-output scratch for the ESD sums
     }
     if (need_xch > h->xch_cap) {
         if (h->d_xch) { cudaDeviceSynchronize(); cudaFree(h->d_xch); h->d_xch = nullptr; h->xch_cap = 0; }
@@ -212,6 +215,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
     for (auto& g : groups)
         for (auto& d : g.d) {
             if (g.C > 1) { d.xch = h->d_xch + xoff; xoff += 2 * (size_t)g.M * g.C; }
+            if (d.esd && !d.hist) { d.xs = h->d_xch + xoff; xoff += (size_t)g.M * g.C; }
             all.push_back(d);
         }
     size_t nb = all.size() * sizeof(PulseDev);
@@ -250,7 +254,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         Group& g = groups[gi];
         const int M = g.M, C = g.C;
-        const KernelEntry* ke = find_kernel(M, C, method);
+        const KernelEntry* ke = find_kernel(M, C, vc.nee ? kHeunNee : method);
         if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
                              "no kernel for cta_points=" + std::to_string(M) + " cluster=" + std::to_string(C));
         const FftTables tabs = tabv[gi];
@@ -267,7 +271,6 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         cfg.shared_sched = shared ? 1 : 0;
         cfg.max_attempts_mul = 64;
         cfg.grid_flags = h->d_grid_flags;
-        cfg.nee = vc.nee;
         cudaStream_t ls = st;
         if (gi > 0) {
             ls = h->side[gi - 1];

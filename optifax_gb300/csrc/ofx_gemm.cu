@@ -113,25 +113,43 @@ __global__ void __launch_bounds__(128, 1)
     }
     __syncwarp();
 
-    // epilogue: TMEM lane (32 warp + lane) holds output row m0 + 32 warp + lane
+    // epilogue: TMEM lane (32 warp + lane) holds output row m0 + 32 warp + lane.  The
+    // tile goes through shared memory (the drained stage buffers: every TMA load was
+    // consumed by an MMA before the accumulator barrier completed) so that the global
+    // stores run along rows: one warp writes two 256-byte row segments per store.
     const bool ok = mbar_wait(accum, 0) && !*(volatile int*)abort_flag;
     __syncwarp();
     tc_fence_after();
-    const int row = m0 + warp * 32 + lane;
+    constexpr int LDT = BN + 1;                          // padded row: conflict-free column writes
+    float* tile = reinterpret_cast<float*>(tiles);
     const uint32_t taddr = tmem + (static_cast<uint32_t>(warp * 32) << 16);
+    const int trow = warp * 32 + lane;
 #pragma unroll
     for (int c = 0; c < BN; c += 16) {
         float v[16];
         tmem_ld16(taddr + c, v);
-        if (ok && row < g.M) {
-            float* crow = g.C + static_cast<long long>(row) * g.ldc;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int col = n0 + c + j;
-                if (col < g.N) {
-                    if (g.atomic) atomicAdd(crow + col, v[j]);
-                    else crow[col] = v[j];
-                }
+        for (int j = 0; j < 16; ++j) tile[trow * LDT + c + j] = v[j];
+    }
+    __syncthreads();
+    if (ok) {
+        const bool vec = !g.atomic && (g.ldc % 4 == 0) && (n0 + BN <= g.N) &&
+                         ((reinterpret_cast<uintptr_t>(g.C) & 15) == 0);
+        for (int idx = threadIdx.x; idx < BM * (BN / 4); idx += blockDim.x) {
+            const int r = idx / (BN / 4), c4 = (idx % (BN / 4)) * 4;
+            const int row = m0 + r;
+            if (row >= g.M) continue;
+            float* dst = g.C + static_cast<long long>(row) * g.ldc + n0 + c4;
+            const float* src = tile + r * LDT + c4;
+            if (vec) {
+                *reinterpret_cast<float4*>(dst) = make_float4(src[0], src[1], src[2], src[3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (n0 + c4 + j < g.N) {
+                        if (g.atomic) atomicAdd(dst + j, src[j]);
+                        else dst[j] = src[j];
+                    }
             }
         }
     }

@@ -19,5 +19,6 @@ KernelEntry kernel_entry() {
 void register_kernels_heun_large(std::vector<KernelEntry>& v);
 void register_kernels_heun_small(std::vector<KernelEntry>& v);
 void register_kernels_rk23(std::vector<KernelEntry>& v);
+void register_kernels_heun_nee(std::vector<KernelEntry>& v);
 
 }  // namespace ofx

@@ -66,6 +66,7 @@ struct PulseDev {
     float* esd;
     int n_esd;
     float* smt;              // optional per-trip stepmods records (n_trips x S)
+    float2* xs;              // trip-output scratch (N) for the ESD sums when hist is not given
     // cluster (C > 1) exchange scratch in global memory: 2 N complex
     float2* xch;
 };
@@ -83,8 +84,12 @@ struct KernelCfg {
     int shared_sched;    // 1: OR the error flags over every pulse of the launch (grid barrier)
     int max_attempts_mul;
     int* grid_flags;     // 3 ints (shared schedule only)
-    int nee;             // NEE_CPU.m step control (Heun only)
 };
+
+// Kernel flavours: the MEX Heun and RK23 schedules (OPTIFAX_HEUN, OPTIFAX_RK23) and
+// the Heun schedule with NEE_CPU.m step control, a separate instantiation so the
+// MEX kernels carry no NEE branches.
+constexpr int kHeunNee = 2;
 
 // ---------------------------------------------------------------------------
 // pointwise physics
@@ -217,7 +222,7 @@ struct Smem {
     static constexpr size_t off_papp = off_l2a + sizeof(float) * M;
     static constexpr size_t off_abc = off_papp + sizeof(uint32_t) * M;
     // Heun: per-mode D - 1 and its fixed-point phase increment for the cached stepmod
-    static constexpr int NCACHE = (METHOD == OPTIFAX_HEUN) ? M : 0;
+    static constexpr int NCACHE = (METHOD != OPTIFAX_RK23) ? M : 0;
     static constexpr size_t off_dmc = off_abc + sizeof(float) * M;
     static constexpr size_t off_dfc = off_dmc + sizeof(float2) * NCACHE;
     static constexpr size_t off_edge = off_dfc + sizeof(int) * NCACHE;
@@ -475,7 +480,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
     const int n_trips = P.n_trips > 0 ? P.n_trips : 1;
     const bool rec = (c == 0 && t == 0);
 
-    const bool nee = cfg.nee != 0;           // NEE_CPU.m: k is 1-based, no chunk clamp
+    constexpr bool nee = (METHOD == kHeunNee);   // NEE_CPU.m: k is 1-based, no chunk clamp
+    constexpr bool heun = (METHOD != OPTIFAX_RK23);
     float k = nee ? 1.f : 0.f, stepprev = 4.f, stepmod = 4.f;
     unsigned q = 0;                          // accumulated dispersion position (sum of stepmod)
     int s_cached = -1;                       // stepmod of the cached per-mode D - 1 (Heun)
@@ -517,7 +523,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                 const float hmod = stepmod * h;
                 const float hg = hmod * G[kidx];
                 int bits = 0;
-                if constexpr (METHOD == OPTIFAX_HEUN) {
+                if constexpr (heun) {
                     // ---- stage 1: K1 = f(A0) at z = k ----
                     float2 nl[16], k1[16], L, R;
                     float2 z = zphase(P.tau_z4, kpos);
@@ -638,7 +644,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                         stepprev = stepmod;
                         stepmod = stepend;
                     } else {
-                        if constexpr (METHOD == OPTIFAX_HEUN) {
+                        if constexpr (heun) {
                             if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.f) < cend - 1.f) stepmod = stepmod + 1.f;
                         } else {
                             if (!(fl & 2) && !(fl & 1) && (k + stepmod + stepmod) < cend - 1.f) stepmod = stepmod * 2.f;
@@ -668,6 +674,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     fft_forward_to_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
                     float part[4] = {0.f, 0.f, 0.f, 0.f};
+                    // crystal output of the trip (history row, or scratch for the ESD sums)
+                    float2* const xsp = !cav ? nullptr : (P.hist ? P.hist + (size_t)trip * N : P.xs);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         // phase increment beta*s from the exact fixed-point target minus the
@@ -681,7 +689,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                         int d32 = (int)((long long)(target - ((uint64_t)ph << 32)) >> 32);
                         float2 dm1;
                         int dused;
-                        if constexpr (METHOD == OPTIFAX_HEUN) {
+                        if constexpr (heun) {
                             // D - 1 cached per mode for the current stepmod; the small
                             // difference eps between the wanted and the cached increment
                             // is applied to first order: D e^{-i eps} - 1 ~ (D - 1) - i eps D
@@ -713,19 +721,26 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
 #pragma unroll
                             for (int i = 0; i < 4; ++i)
                                 if (i < P.n_tally) part[i] = fmaf(P.tally_w[(size_t)i * N + kk], x2, part[i]);
-                            if (P.hist) P.hist[(size_t)trip * N + kk] = X;
-                            if (P.esd) {
-                                // every mode has one owner thread: plain read-modify-write
-#pragma unroll
-                                for (int i = 0; i < 4; ++i)
-                                    if (i < P.n_esd) P.esd[(size_t)i * N + kk] += P.esd_w[(size_t)i * N + kk] * x2;
-                            }
+                            if (xsp) xsp[kk] = X;
                             v[j] = cadd(cmul(X, P.fb[kk]), P.pump[kk]);
                         } else {
                             v[j] = cmul(eh, dm1);
                         }
                     }
                     s_cached = s_used;
+                    if (cav && P.esd) {
+                        // ESD trip sums from the stored crystal output, outside the unrolled
+                        // mode loop; every mode has one owner thread (plain read-modify-write)
+#pragma unroll 1
+                        for (int j = 0; j < 16; ++j) {
+                            const int kk = c + C * bitrev(16 * t + j, LOG2M);
+                            const float2 X = xsp[kk];
+                            const float x2 = X.x * X.x + X.y * X.y;
+#pragma unroll 1
+                            for (int i = 0; i < P.n_esd; ++i)
+                                P.esd[(size_t)i * N + kk] += P.esd_w[(size_t)i * N + kk] * x2;
+                        }
+                    }
                     fft_inverse_from_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     if constexpr (C > 1) {
                         cg::this_cluster().sync();
