@@ -201,7 +201,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         n_desc += g.d.size();
         if (g.C > 1) need_xch += g.d.size() * 2 * (size_t)g.M * g.C;
         for (const auto& d : g.d)
-            if (d.esd && !d.hist) need_xch += (size_t)g.M * g.C;    // trip-output scratch for the ESD sums
+            if (d.fb) need_xch += (size_t)g.M * g.C;    // OPO: the trip's crystal output (cavity scratch)
     }
     if (need_xch > h->xch_cap) {
         if (h->d_xch) { cudaDeviceSynchronize(); cudaFree(h->d_xch); h->d_xch = nullptr; h->xch_cap = 0; }
@@ -215,7 +215,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
     for (auto& g : groups)
         for (auto& d : g.d) {
             if (g.C > 1) { d.xch = h->d_xch + xoff; xoff += 2 * (size_t)g.M * g.C; }
-            if (d.esd && !d.hist) { d.xs = h->d_xch + xoff; xoff += (size_t)g.M * g.C; }
+            if (d.fb) { d.xs = h->d_xch + xoff; xoff += (size_t)g.M * g.C; }
             all.push_back(d);
         }
     size_t nb = all.size() * sizeof(PulseDev);

@@ -674,8 +674,9 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     fft_forward_to_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
                     float part[4] = {0.f, 0.f, 0.f, 0.f};
-                    // crystal output of the trip (history row, or scratch for the ESD sums)
-                    float2* const xsp = !cav ? nullptr : (P.hist ? P.hist + (size_t)trip * N : P.xs);
+                    // the trip's crystal output goes to the cavity scratch; the cavity
+                    // work (tallies, ESD sums, history, transfer) runs after the loop
+                    float2* const xsp = cav ? P.xs : nullptr;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         // phase increment beta*s from the exact fixed-point target minus the
@@ -715,31 +716,31 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                         float2 eh = v[j];
                         int kk = c + C * bitrev(16 * t + j, LOG2M);
                         if (apc) apc[kk] = cadd(eh, cmul(eh, dm1));
-                        if (cav) {
-                            float2 X = cadd(eh, cmul(eh, dm1));
-                            float x2 = X.x * X.x + X.y * X.y;
-#pragma unroll
-                            for (int i = 0; i < 4; ++i)
-                                if (i < P.n_tally) part[i] = fmaf(P.tally_w[(size_t)i * N + kk], x2, part[i]);
-                            if (xsp) xsp[kk] = X;
-                            v[j] = cadd(cmul(X, P.fb[kk]), P.pump[kk]);
-                        } else {
-                            v[j] = cmul(eh, dm1);
-                        }
+                        if (cav) xsp[kk] = cadd(eh, cmul(eh, dm1));
+                        else v[j] = cmul(eh, dm1);
                     }
                     s_cached = s_used;
-                    if (cav && P.esd) {
-                        // ESD trip sums from the stored crystal output, outside the unrolled
-                        // mode loop; every mode has one owner thread (plain read-modify-write)
+                    if (cav) {
+                        // once per round trip, outside the unrolled mode loop (code size is
+                        // this kernel's bound): energy tallies, ESD sums and history of the
+                        // crystal output X, then Y = X fb + pump; every mode has one owner
+                        // thread, which reads back only what it wrote
 #pragma unroll 1
                         for (int j = 0; j < 16; ++j) {
                             const int kk = c + C * bitrev(16 * t + j, LOG2M);
                             const float2 X = xsp[kk];
                             const float x2 = X.x * X.x + X.y * X.y;
+#pragma unroll
+                            for (int i = 0; i < 4; ++i)
+                                if (i < P.n_tally) part[i] = fmaf(P.tally_w[(size_t)i * N + kk], x2, part[i]);
 #pragma unroll 1
                             for (int i = 0; i < P.n_esd; ++i)
                                 P.esd[(size_t)i * N + kk] += P.esd_w[(size_t)i * N + kk] * x2;
+                            if (P.hist) P.hist[(size_t)trip * N + kk] = X;
+                            xsp[kk] = cadd(cmul(X, P.fb[kk]), P.pump[kk]);
                         }
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) v[j] = xsp[c + C * bitrev(16 * t + j, LOG2M)];
                     }
                     fft_inverse_from_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     if constexpr (C > 1) {
