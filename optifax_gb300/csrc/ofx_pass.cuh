@@ -670,6 +670,20 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     } else {
                         __syncthreads();
                     }
+                    if constexpr (heun) {
+                        // refresh the per-mode D - 1 cache when the step size changed (a
+                        // compact loop: kept out of the unrolled mode loop below)
+                        if (s_used != s_cached) {
+#pragma unroll 1
+                            for (int j = 0; j < 16; ++j) {
+                                const int idx = j * T + t;
+                                int dc;
+                                const uint64_t inc = tau_s[idx] * (uint64_t)(unsigned)s_used;
+                                dmc_s[idx] = dispersion_dm1((int)((long long)inc >> 32), l2a_s[idx], s_used, &dc);
+                                dfc_s[idx] = dc;
+                            }
+                        }
+                    }
                     float2 v[16];
                     fft_forward_to_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
@@ -694,12 +708,6 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                             // D - 1 cached per mode for the current stepmod; the small
                             // difference eps between the wanted and the cached increment
                             // is applied to first order: D e^{-i eps} - 1 ~ (D - 1) - i eps D
-                            if (s_used != s_cached) {
-                                int dc;
-                                uint64_t inc = tau_s[idx] * (uint64_t)(unsigned)s_used;
-                                dmc_s[idx] = dispersion_dm1((int)((long long)inc >> 32), l2a_s[idx], s_used, &dc);
-                                dfc_s[idx] = dc;
-                            }
                             float2 dc1 = dmc_s[idx];
                             int eps = d32 - dfc_s[idx];
                             dm1 = dc1;
