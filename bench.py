@@ -215,43 +215,60 @@ def run_sweep(args):
     A step is one whole batch; value = instances per second."""
     import numpy as np
     import torch
-    from optifax_gb300 import sweep, solver as sv
-    insts = sweep.config3_instances(n=args.sweep_size, seed=2)
-    t0 = time.perf_counter()
-    inputs = [sweep.build_inputs(i) for i in insts]
-    prep_s = time.perf_counter() - t0
-    sweep.build_specs_device(insts[:4])            # warm-up (library load, twiddles)
+    from optifax_gb300 import sweep, solver as sv, dist, physics as ph
+    rank, world, local = dist.init("nccl")
+    torch.cuda.set_device(local)
+    all_insts = sweep.config3_instances(n=args.sweep_size, seed=2)
+    # independent passes: contiguous instance ranges balanced by N log2(N) S per rank
+    costs = [dist.pass_cost(i.n_points, ph.Crystal(i.length, i.period).n_steps) for i in all_insts]
+    part = dist.partition_by_cost(costs, world)[rank]
+    insts = [all_insts[i] for i in part]
+    prep_s = 0.0
+    if rank == 0 and world == 1:
+        t0 = time.perf_counter()
+        [sweep.build_inputs(i) for i in insts]          # host precompute, timed for comparison
+        prep_s = time.perf_counter() - t0
+    sweep.build_specs_device(insts[:4], device=local)   # warm-up (library load, twiddles)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    specs = sweep.build_specs_device(insts)        # the same inputs, computed on the device
+    specs = sweep.build_specs_device(insts, device=local)   # the solver inputs, computed on the device
     prep_dev_s = time.perf_counter() - t0
-    tuned = sv.autotune(sorted({i.n_points for i in insts}))
+    tuned = sv.autotune(sorted({i.n_points for i in insts}), device=local)
     stream = torch.cuda.current_stream()
-    for _ in range(1):
-        sv.propagate(specs, stream=stream)
+    sv.propagate(specs, stream=stream)
     torch.cuda.synchronize()
     times, atts = [], []
-    with ClockSampler(0) as clk:
+    with ClockSampler(local) as clk:
         for _ in range(args.steps):
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            dist.barrier()
+            torch.cuda.synchronize()
             ev0.record(stream)
             _, st = sv.propagate(specs, stream=stream)
             ev1.record(stream)
             torch.cuda.synchronize()
-            times.append(ev0.elapsed_time(ev1) / 1000.0)
+            dist.barrier()
+            times.append(dist.max_over_ranks(ev0.elapsed_time(ev1) / 1000.0, torch.device("cuda", local)))
             atts.append(sv.decode_stats(st))
     t = float(np.mean(times))
     stats = atts[-1]
-    point_attempts = sum(s_["attempts"] * i.n_points for s_, i in zip(stats, insts))
+    local_pa = sum(s_["attempts"] * i.n_points for s_, i in zip(stats, insts))
+    local_att = int(sum(s_["attempts"] for s_ in stats))
+    gathered = dist.gather_to_rank0({"point_attempts": local_pa, "attempts": local_att, "n": len(insts)})
+    if rank != 0:
+        return
+    point_attempts = sum(g["point_attempts"] for g in gathered)
+    attempts = sum(g["attempts"] for g in gathered)
     peak, peak_kind = _peaks()
     achieved = 16.0 * point_attempts / t / 1e9
-    line = {"metric": "batched crystal passes/s (uneven sweep)", "value": len(insts) / t, "unit": "passes/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": t * 1000.0, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"config 3 sweep: {len(insts)} instances, N 2^12..2^16, L 0.5-10 mm, "
+    line = {"metric": "batched crystal passes/s (uneven sweep)", "value": len(all_insts) / t, "unit": "passes/s",
+            "n_gpus": world, "steps": args.steps, "warmup": 1, "ms_per_step": t * 1000.0, "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"config 3 sweep: {len(all_insts)} instances, N 2^12..2^16, L 0.5-10 mm, "
                                    "period 28-32 um, 0.5-3 W, 100-300 fs, seed 2", "autotuned_cta_points": tuned,
+                       "parallelism": f"{world} rank(s), contiguous instance ranges balanced by N log2(N) S",
                        "host_prep_s": prep_s, "device_prep_s": prep_dev_s, "point_attempts": point_attempts,
-                       "attempts": int(sum(s_["attempts"] for s_ in stats))},
+                       "attempts": attempts},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                          "algorithmic": "16 B per grid point per step attempt"},
