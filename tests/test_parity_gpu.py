@@ -97,6 +97,16 @@ def test_heun_xtal_single_pulse(oracle, N, cta):
     print(info)
 
 
+@pytest.mark.parametrize("N,length", [(32768, 0.05e-3), (65536, 0.03e-3)])
+def test_heun_large_clusters(oracle, N, length):
+    """Clusters of 8 and 16 CTAs (4096 points each): the sweep's and the precision
+    study's largest grids."""
+    from optifax_gb300 import _native as nat
+    win, si, E = make_case(N=N, length=length, power=2.0)
+    info = check_parity(oracle, si, E[0], nat.HEUN, nat.VARIANT_BATCH_XTAL, 4096)
+    print(info)
+
+
 @pytest.mark.parametrize("variant", [2, 3])
 def test_heun_legacy_variants(oracle, variant):
     from optifax_gb300 import _native as nat
@@ -104,7 +114,7 @@ def test_heun_legacy_variants(oracle, variant):
     check_parity(oracle, si, E[0], nat.HEUN, variant)
 
 
-@pytest.mark.parametrize("N,cta", [(1024, 0), (2048, 1024)])
+@pytest.mark.parametrize("N,cta", [(1024, 0), (2048, 1024), (16384, 4096)])
 def test_rk23_ode23(oracle, N, cta):
     from optifax_gb300 import _native as nat
     win, si, E = make_case(N=N, length=0.2e-3, power=2.0)
