@@ -30,6 +30,11 @@ WORKLOAD = ("SPOPO round trips: N=2^14 over 12 ps, 5 mm MgO:PPLN 30 um, sech2 10
             "10% OC, signal-band feedback, delay 0, noise seed 1")
 
 
+# DRAM bytes per OPO round trip of pass_kernel<4096, 4, HEUN>: ncu dram__bytes_read.sum
+# (2,148,096) + dram__bytes_write.sum (206,336) of the bench's timed 10-trip launch
+TRAFFIC_PER_TRIP = (2148096 + 206336) / 10.0
+
+
 def _spec():
     from optifax_gb300.opo import CavitySpec
     return CavitySpec(n_points=2 ** 14, window=12e-12, crystal_length=5e-3, period=30e-6,
@@ -411,7 +416,10 @@ def main():
                        "attempts_timed": attempts,
                        "l2": "flushed (256 MB write) before the timed launch; the field stays on-chip by design"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak, "traffic": TRAFFIC_PER_TRIP * K,
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the timed "
+                                           "launch at 10 trips (2.35 MB), per trip x trips: the field stays "
+                                           "on chip, so real DRAM traffic is tables and per-step G reads",
                          "peak_kind": peak_kind,
                          "algorithmic": "16 B per grid point per step attempt",
                          "compute_tflops": flops_per_launch / (t_max / 1000.0) / 1e12},
