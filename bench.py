@@ -1,6 +1,6 @@
 """Benchmark: synchronously pumped OPO round trips per second on one GB300.
 
-Workload (BASELINE config 2): SPOPO with a 2^14-point grid over 12 ps, 5 mm
+Workload: SPOPO with a 2^14-point grid over 12 ps, 5 mm
 MgO:PPLN (30 um period, d_eff 14 pm/V), sech^2 pump 1040 nm / 200 fs / 2 W /
 100 MHz / 15 um waist, signal-band feedback, 10 % output coupler, zero delay,
 one-photon-per-mode noise seed 1.  A step is one round trip (crystal pass +
@@ -223,7 +223,7 @@ def run_sweep(args):
     from optifax_gb300 import sweep, solver as sv, dist, physics as ph
     rank, world, local = dist.init("nccl")
     torch.cuda.set_device(local)
-    all_insts = sweep.config3_instances(n=args.sweep_size, seed=2)
+    all_insts = sweep.uneven_sweep_instances(n=args.sweep_size, seed=2)
     # independent passes: contiguous instance ranges balanced by N log2(N) S per rank
     costs = [dist.pass_cost(i.n_points, ph.Crystal(i.length, i.period).n_steps) for i in all_insts]
     part = dist.partition_by_cost(costs, world)[rank]
@@ -269,7 +269,7 @@ def run_sweep(args):
     line = {"metric": "batched crystal passes/s (uneven sweep)", "value": len(all_insts) / t, "unit": "passes/s",
             "n_gpus": world, "steps": args.steps, "warmup": 1, "ms_per_step": t * 1000.0, "higher_is_better": True,
             "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"config 3 sweep: {len(all_insts)} instances, N 2^12..2^16, L 0.5-10 mm, "
+            "config": {"workload": f"uneven sweep: {len(all_insts)} instances, N 2^12..2^16, L 0.5-10 mm, "
                                    "period 28-32 um, 0.5-3 W, 100-300 fs, seed 2", "autotuned_cta_points": tuned,
                        "parallelism": f"{world} rank(s), contiguous instance ranges balanced by N log2(N) S",
                        "host_prep_s": prep_s, "device_prep_s": prep_dev_s, "point_attempts": point_attempts,
@@ -291,7 +291,7 @@ def main():
     ap.add_argument("--cta-points", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="opo", choices=["opo", "sweep"],
-                    help="opo: config-2 OPO round trips (default line); sweep: config-3 batched passes")
+                    help="opo: 2^14-point SPOPO round trips (default line); sweep: 256 uneven batched passes")
     ap.add_argument("--sweep-size", type=int, default=256)
     ap.add_argument("--fp64-trips", type=int, default=1,
                     help="round trips of the plain FP64 solver timed beside the line (0: skip)")

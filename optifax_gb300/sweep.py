@@ -1,4 +1,4 @@
-"""Batched crystal-pass sweeps with uneven grids and crystals (BASELINE config 3).
+"""Batched crystal-pass sweeps with uneven grids and crystals: 256 instances, N 2^12..2^16, 0.5-10 mm crystals.
 
 Every instance has its own grid size, crystal length, poling period, pump
 power and pulse width, and its own adaptive step schedule; all run in one
@@ -33,7 +33,7 @@ class Instance:
     seed: int
 
 
-def config3_instances(n: int = 256, seed: int = 2, n_range=(12, 16), length_range=(0.5e-3, 10e-3),
+def uneven_sweep_instances(n: int = 256, seed: int = 2, n_range=(12, 16), length_range=(0.5e-3, 10e-3),
                       period_range=(28e-6, 32e-6), power_range=(0.5, 3.0), tau_range=(100e-15, 300e-15)):
     """Instances drawn with a seeded generator: N uniform over 2^12..2^16 and the
     other parameters uniform over their ranges."""

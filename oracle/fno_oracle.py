@@ -1,6 +1,6 @@
 """FP64 numpy restatement of the crystal-pass surrogate network (forward, loss, backward).
 
-TEST INFRASTRUCTURE ONLY: the checker of the GPU kernels in
+TEST INFRASTRUCTURE ONLY: the oracle for the GPU kernels in
 optifax_gb300/csrc/ofx_fno.cu.  Only tests/ may import it.  The network has no
 counterpart in the reference (OptiFax has no learned component), so this file
 restates the architecture the GPU code implements, with the same parameter

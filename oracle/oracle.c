@@ -1,7 +1,7 @@
 /*
  * oracle.c -- FP64 CPU restatement of OptiFax's chi(2) crystal-pass solver.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU propagator
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle for the GPU propagator
  * in optifax_gb300/csrc/.  Only tests/, __graft_entry__.smoke() and bench.py
  * (its cpu_baseline leg and its --impl reference arm) may load it.  The
  * product path never calls it.

@@ -10,7 +10,7 @@ import torch.multiprocessing as mp
 
 def test_partition_balances_and_covers():
     from optifax_gb300 import dist, sweep
-    insts = sweep.config3_instances(n=64, seed=2)
+    insts = sweep.uneven_sweep_instances(n=64, seed=2)
     from optifax_gb300 import physics as ph
     costs = [dist.pass_cost(i.n_points, ph.Crystal(i.length, i.period).n_steps) for i in insts]
     for world in (1, 2, 3, 8):

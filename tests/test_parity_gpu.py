@@ -1,6 +1,6 @@
 """GPU crystal pass vs the FP64 oracle (parity).  Marked gpu.
 
-Tolerances (spec bar): relative L2 error of the output field <= 1e-4,
+Tolerances: relative L2 error of the output field <= 1e-4,
 relative pulse-energy error <= 1e-6, bit-identical step schedules.  When the
 FP32 and FP64 error norms fall on opposite sides of a threshold the
 schedules fork; the oracle then replays the GPU's decisions (the decision
