@@ -128,9 +128,42 @@ def cpu_oracle_sample(spec, fraction=0.05, threads=1, field=None, attempts_per_t
                       f"({att} attempts, {el:.1f} s), {how}"}
 
 
+def reference_gpu_sample(spec, fraction=0.1):
+    """The reference's own CUDA kernels (OPO_CUDA_BATCH_XTAL.cu compiled unmodified,
+    driven with cuFFT as its MEX driver does) on the first `fraction` of one crystal
+    pass from the first trip's input; the time per attempt, scaled to a built-up
+    round trip (0.97 attempts per z-sample), bounds the reference's round trips/s
+    from above (its cavity step runs on the host in MATLAB and is not counted)."""
+    import numpy as np
+    from oracle import ref_mex
+    from optifax_gb300.opo import build_cavity
+    ok, why = ref_mex.available()
+    if not ok:
+        return {"unavailable": why}
+    arr = build_cavity(spec)
+    si = arr.si
+    S = max(8, int(si.n_steps * fraction))
+    sel = float(np.ceil(S / 4))
+    ref_mex.run(arr.E0, si.alpha, si.G[:S // 10], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                n_steps=S // 10, dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=sel / 10,
+                trace_cap=0)                       # warm-up: module load, cuFFT plan
+    r = ref_mex.run(arr.E0, si.alpha, si.G[:S], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                    n_steps=S, dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=sel, trace_cap=0)
+    per_attempt = r.seconds / r.attempts
+    per_trip = per_attempt * 0.97 * si.n_steps
+    return {"value": 1.0 / per_trip, "unit": UNIT, "us_per_attempt": per_attempt * 1e6,
+            "kind": "reference CUDA kernels (cubin of OPO_CUDA_BATCH_XTAL.cu) + cuFFT, host-driven "
+                    "as OPO_TEST_CUDA: 2 device syncs and a flag read-back per attempt",
+            "sample": f"first {S} of {si.n_steps} steps of one 5 mm pass from the first trip's input "
+                      f"({r.attempts} attempts, {r.seconds:.2f} s), scaled by attempts to a built-up "
+                      f"round trip; crystal pass only (upper bound on round trips/s)"}
+
+
 def run_reference(args):
     """--impl reference: the reference's CPU path restated in C (FP64 oracle);
-    the reference's own CPU code is MATLAB (NEE_CPU.m) and cannot run here."""
+    the reference's own CPU code is MATLAB (NEE_CPU.m) and cannot run here.
+    The line also carries the reference's own CUDA kernels timed on this GPU
+    (``reference_gpu``), where their cubin is present."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -153,6 +186,10 @@ def run_reference(args):
                                        "by attempts to a built-up round trip (0.97 attempts per z-sample, as "
                                        "measured on the GPU); the reference CPU path NEE_CPU.m is MATLAB"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    try:
+        line["reference_gpu"] = reference_gpu_sample(spec)
+    except Exception as exc:  # noqa: BLE001
+        line["reference_gpu"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line))
 
 
