@@ -6,12 +6,15 @@
  * (its cpu_baseline leg and its --impl reference arm) may load it.  The
  * product path never calls it.
  *
- * Parity status: UNPINNED.  The reference ships no golden vectors, fixtures or
- * tests for this path, and its own implementations (MATLAB NEE_CPU.m and the
- * MATLAB MEX wrapper around OPO_CUDA_*.cu) cannot run in this environment.
- * The restatement is instead checked by known-answer tests (pure dispersion,
- * undepleted-pump sinc^2 gain, Manley-Rowe/energy conservation, convergence
- * order) in tests/test_oracle.py.
+ * Parity status: PINNED to the reference's own CUDA kernels.  The reference
+ * ships no golden vectors, fixtures or tests for this path, and its MATLAB
+ * code cannot run here; its MEX kernels (OPO_CUDA_BATCH_XTAL.cu,
+ * ode23/OPO_CUDA_ODE23.cu) are compiled unmodified into cubins and driven with
+ * cuFFT by oracle/ref_mex.cpp.  tests/test_reference_kernels_gpu.py checks this
+ * restatement against them on the GPU: identical step schedules (Heun), and
+ * fields within the drift of cuFFT's FP32 round trips.  Known-answer tests
+ * (pure dispersion, FFT, convergence order, replay, the reject rules) are in
+ * tests/test_oracle.py.  The NEE_CPU.m schedule (MATLAB only) stays unpinned.
  *
  * Three schedules are restated, each in double precision, with every input
  * value taken exactly as the reference receives it (w0, h, G, beta, alpha are

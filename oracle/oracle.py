@@ -2,7 +2,9 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py (cpu_baseline leg and the
 ``--impl reference`` arm) import this module.  The product path in
-optifax_gb300/ never does.  Parity status: unpinned (see oracle.c header).
+optifax_gb300/ never does.  Parity status: pinned to the reference's own CUDA kernels for the
+MEX schedules (oracle/ref_mex.py, tests/test_reference_kernels_gpu.py); the
+NEE_CPU.m schedule is unpinned (see oracle.c header).
 """
 from __future__ import annotations
 
