@@ -8,8 +8,8 @@
  *
  * Parity status: PINNED to the reference's own CUDA kernels.  The reference
  * ships no golden vectors, fixtures or tests for this path, and its MATLAB
- * code cannot run here; its MEX kernels (OPO_CUDA_BATCH_XTAL.cu,
- * ode23/OPO_CUDA_ODE23.cu) are compiled unmodified into cubins and driven with
+ * code cannot run here; its MEX kernels (OPO_CUDA_BATCH_XTAL.cu, _BATCH_OP.cu,
+ * _NO_BC.cu, _HARD_BC.cu, ode23/OPO_CUDA_ODE23.cu) are compiled unmodified into cubins and driven with
  * cuFFT by oracle/ref_mex.cpp.  tests/test_reference_kernels_gpu.py checks this
  * restatement against them on the GPU: identical step schedules (Heun), and
  * fields within the drift of cuFFT's FP32 round trips.  Known-answer tests

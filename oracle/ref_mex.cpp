@@ -87,7 +87,17 @@ const char* refmex_last_error() { return g_err.c_str(); }
 
 /*
  * One MEX crystal pass (OPO_mex_BATCH.cpp:41-122 + OPO_CUDA_BATCH_XTAL.cu:373-524)
- * on B pulses of N points.  Host arrays:
+ * on B pulses of N points.  variant selects the driver of the cubin passed:
+ *   0 BATCH_XTAL  (G row per pulse: KN_kernel takes Nsteps, :195-252; float sel,
+ *                  chunk count rounded up, k < Nsteps guard, absorber 6N/16..10N/16)
+ *   1 BATCH_OP    (OPO_CUDA_BATCH_OP.cu:372-520: as XTAL with one shared G,
+ *                  KN_kernel without Nsteps, :197-221)
+ *   2 NO_BC       (OPO_CUDA_NO_BC.cu:364-510: int sel, truncated chunk count (:397),
+ *                  no guard, absorber range empty (:401-402))
+ *   3 HARD_BC     (OPO_CUDA_HARD_BC.cu:365-509: as NO_BC with the absorber range
+ *                  of XTAL (:400-401); its complex_ScaleVec zeroes it, :105-129)
+ * The time convention and the absorber's shape are inside each file's kernels.
+ * Host arrays:
  *   E[B*N] (float2 as interleaved floats), alpha[N], G[S*B], beta[N] -- the
  *   MEX inputs 0, 1, 2, 8;  Ap[nchunks*N*B] and stepmods[S] are in/out
  *   (inputs 12 and 13, copied in and returned as the reference does);
@@ -96,7 +106,7 @@ const char* refmex_last_error() { return g_err.c_str(); }
  * forced (optional decisions), seconds (wall time of the pass on the device).
  * Returns 0, or -1 with refmex_last_error() set.
  */
-int refmex_run(const char* cubin, const float* E, int N, int B, const float* alpha, const float* G,
+int refmex_run(const char* cubin, int variant, const float* E, int N, int B, const float* alpha, const float* G,
                const float* beta, float w0, double bdiffw0, float h, int S, double dt,
                float max_pct_err, float min_pct_err, float sel, float* Ap, long long ap_len,
                float* stepmods, float* A_out, int* trace, int trace_cap, int* n_attempts,
@@ -105,13 +115,20 @@ int refmex_run(const char* cubin, const float* E, int N, int B, const float* alp
     if (N < kThreads || N % kThreads != 0 || B < 1 || S < 1 || !(sel > 0.f))
         return set_err("refmex_run: N must be a multiple of 128 (KN_kernel has no bounds guard), B, S, sel > 0", 0), -1;
 
-    // chunk count as the driver computes it (:403-407)
+    if (variant < 0 || variant > 3) return set_err("refmex_run: variant must be 0..3", variant), -1;
+    const bool g_rows = (variant == 0);              // KN_kernel(..., Nsteps, ...) and G[k + row S]
+    const bool int_sel = (variant >= 2);             // int sel, truncated chunks, no k < Nsteps guard
+    if (int_sel) sel = (float)(int)sel;
+    if (!(sel >= 1.f)) return set_err("refmex_run: sel < 1", 0), -1;
+    // chunk count as each driver computes it (XTAL :403-407; NO_BC :397)
     int nchunks = (int)((float)S / sel);
-    if ((float)nchunks * sel < (float)S) nchunks += 1;
+    if (int_sel) nchunks = S / (int)sel;
+    else if ((float)nchunks * sel < (float)S) nchunks += 1;
     if (ap_len < (long long)nchunks * N * B * 2)
         return set_err("refmex_run: Ap holds fewer than nchunks*N*B complex values", nchunks), -1;
 
     const size_t fb = sizeof(float) * 2 * (size_t)N * B;
+    const size_t g_len = g_rows ? (size_t)S * B : (size_t)S;
     CUmodule mod = nullptr;
     cufftHandle plan = 0;
     bool have_plan = false;
@@ -130,7 +147,7 @@ int refmex_run(const char* cubin, const float* E, int N, int B, const float* alp
 
     RT(cudaMalloc(&dE, fb)); RT(cudaMalloc(&dA0, fb)); RT(cudaMalloc(&dA1, fb));
     RT(cudaMalloc(&dNL, fb)); RT(cudaMalloc(&dK1, fb)); RT(cudaMalloc(&dK2, fb));
-    RT(cudaMalloc(&dG, sizeof(float) * (size_t)S * B));
+    RT(cudaMalloc(&dG, sizeof(float) * g_len));
     RT(cudaMalloc(&dal, sizeof(float) * N)); RT(cudaMalloc(&dbe, sizeof(float) * N));
     RT(cudaMalloc(&dAp, sizeof(float) * (size_t)ap_len));
     RT(cudaMalloc(&dsm, sizeof(float) * (size_t)S));
@@ -138,7 +155,7 @@ int refmex_run(const char* cubin, const float* E, int N, int B, const float* alp
     // E and A0 both start as copies of the input (OPO_mex_BATCH.cpp:41,86)
     RT(cudaMemcpy(dE, E, fb, cudaMemcpyHostToDevice));
     RT(cudaMemcpy(dA0, E, fb, cudaMemcpyHostToDevice));
-    RT(cudaMemcpy(dG, G, sizeof(float) * (size_t)S * B, cudaMemcpyHostToDevice));
+    RT(cudaMemcpy(dG, G, sizeof(float) * g_len, cudaMemcpyHostToDevice));
     RT(cudaMemcpy(dal, alpha, sizeof(float) * N, cudaMemcpyHostToDevice));
     RT(cudaMemcpy(dbe, beta, sizeof(float) * N, cudaMemcpyHostToDevice));
     RT(cudaMemcpy(dAp, Ap, sizeof(float) * (size_t)ap_len, cudaMemcpyHostToDevice));
@@ -151,7 +168,8 @@ int refmex_run(const char* cubin, const float* E, int N, int B, const float* alp
         // FP32 driver scalars, as declared in OPO_TEST_CUDA (:395-407)
         const float invdt2 = (float)(1.0 / (2.0 * dt));
         const float invSize = (float)(1.0 / N);
-        const int gi1 = (int)(6.0 * (N / 16)), gi2 = (int)(10.0 * (N / 16));
+        const int gi1 = (variant == 2) ? 0 : (int)(6.0 * (N / 16));
+        const int gi2 = (variant == 2) ? 0 : (int)(10.0 * (N / 16));
         const float one = 1.0f, half = 0.5f;
         float k = 0.f, stepprev = 4.f, stepmod = 4.f, hmod = 0.f;
         const long long max_attempts = 64LL * S + 1024;
@@ -159,7 +177,7 @@ int refmex_run(const char* cubin, const float* E, int N, int B, const float* alp
         for (int chunk = 0; chunk < nchunks; ++chunk) {
             stepmod = stepprev;
             hmod = stepmod * h;
-            for (; k < (float)(chunk + 1) * sel && k < (float)S; k = k + stepmod) {
+            for (; k < (float)(chunk + 1) * sel && (int_sel || k < (float)S); k = k + stepmod) {
                 if (attempt >= max_attempts) { set_err("refmex_run: attempt limit", attempt); goto fail; }
                 const int ki = (int)k, si = (int)stepmod;
                 // stage 1 at z = k h, stage 2 at z = (k + stepmod) h (:431-446)
@@ -170,13 +188,17 @@ int refmex_run(const char* cubin, const float* E, int N, int B, const float* alp
                     int Sv = S;
                     void* a2[] = {&dA0, &dK1, &dK1, &dNL, &dG, &w0, &hmod, (void*)&ki, (void*)&invdt2,
                                   &N, &Sv, &dA1, (void*)&half};
-                    if (!launch(fns[1].f, N, B, a2)) goto fail;
+                    void* a2s[] = {&dA0, &dK1, &dK1, &dNL, &dG, &w0, &hmod, (void*)&ki, (void*)&invdt2,
+                                   &N, &dA1, (void*)&half};
+                    if (!launch(fns[1].f, N, B, g_rows ? a2 : a2s)) goto fail;
                     bdwz = bdiffw0 * (double)(k + stepmod) * (double)h;
                     void* a3[] = {&dNL, &dA1, &dA1, (void*)&dt, &w0, &bdwz, &N};
                     if (!launch(fns[0].f, N, B, a3)) goto fail;
                     void* a4[] = {&dA0, &dK2, &dK1, &dNL, &dG, &w0, &hmod, (void*)&ki, (void*)&invdt2,
                                   &N, &Sv, &dE, (void*)&half};
-                    if (!launch(fns[1].f, N, B, a4)) goto fail;
+                    void* a4s[] = {&dA0, &dK2, &dK1, &dNL, &dG, &w0, &hmod, (void*)&ki, (void*)&invdt2,
+                                   &N, &dE, (void*)&half};
+                    if (!launch(fns[1].f, N, B, g_rows ? a4 : a4s)) goto fail;
                 }
                 RT(cudaDeviceSynchronize());
                 RT(cudaMemset(dflag, 0, 2));

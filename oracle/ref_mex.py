@@ -1,12 +1,13 @@
 """ctypes binding of ref_mex.cpp: the reference's own CUDA kernels on the GPU
 (TEST INFRASTRUCTURE ONLY; tests/ and bench.py load it, the product never does).
 
-The kernels come from OPO_CUDA_BATCH_XTAL.cu compiled unmodified into
-oracle/_ref/opo_cuda_batch_xtal.cubin (oracle/Makefile, target ``ref``, built
-where the reference source is present and shipped as a file); ref_mex.cpp drives
-them with cuFFT as the MEX driver OPO_TEST_CUDA (:373-524) does.  ``run`` takes
-the MEX's inputs in its units (FP32 arrays, FP64 bdiffw0 and dt) and returns its
-three outputs plus the per-attempt decision trace.
+The kernels come from the MEX files OPO_CUDA_{BATCH_XTAL,BATCH_OP,NO_BC,HARD_BC}.cu
+and ode23/OPO_CUDA_ODE23.cu compiled unmodified into oracle/_ref/*.cubin
+(oracle/Makefile, target ``ref``, built where the reference source is present and
+shipped as files); ref_mex.cpp drives them with cuFFT as the MEX drivers
+OPO_TEST_CUDA do.  ``run`` / ``run_ode23`` take the MEX's inputs in its units (FP32
+arrays, FP64 bdiffw0 and dt) and return its three outputs plus the per-attempt
+decision trace.
 """
 from __future__ import annotations
 
@@ -20,6 +21,10 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 CUBIN = os.path.join(_HERE, "_ref", "opo_cuda_batch_xtal.cubin")
 CUBIN_ODE23 = os.path.join(_HERE, "_ref", "opo_cuda_ode23.cubin")
+# Heun MEX variants, numbered as optifax_gb300's OPTIFAX_VARIANT_*: BATCH_XTAL,
+# BATCH_OP, NO_BC, HARD_BC
+HEUN_CUBINS = [os.path.join(_HERE, "_ref", f"opo_cuda_{v}.cubin")
+               for v in ("batch_xtal", "batch_op", "no_bc", "hard_bc")]
 _LIB_PATH = os.path.join(_HERE, "_build", "libref_mex.so")
 _lib = None
 
@@ -48,8 +53,11 @@ def lib():
     return _lib
 
 
-def n_chunks(n_steps: int, sel: float) -> int:
-    """Chunk count as the MEX driver computes it in FP32 (:403-407)."""
+def n_chunks(n_steps: int, sel: float, variant: int = 0) -> int:
+    """Chunk count as the MEX driver computes it: FP32 and rounded up for BATCH_XTAL
+    and BATCH_OP (:403-407), integer and truncated for NO_BC and HARD_BC."""
+    if variant >= 2:
+        return int(n_steps) // int(sel)
     s = np.float32(n_steps)
     sel = np.float32(sel)
     n = int(np.float32(s / sel))
@@ -69,18 +77,23 @@ class RefResult:
 
 
 def run(E, alpha, G, beta, *, w0, bdiffw0, h, n_steps, dt, max_err, min_err, sel,
-        Ap=None, stepmods=None, trace_cap=200000, forced=None) -> RefResult:
+        Ap=None, stepmods=None, trace_cap=200000, forced=None, variant=0) -> RefResult:
+    """One Heun MEX pass through the reference's kernels of `variant` (0 BATCH_XTAL,
+    1 BATCH_OP, 2 NO_BC, 3 HARD_BC)."""
     E = np.ascontiguousarray(np.atleast_2d(E), dtype=np.complex64)
     B, N = E.shape
     S = int(n_steps)
-    nch = n_chunks(S, sel)
+    nch = max(n_chunks(S, sel, variant), 1)
     alpha = np.ascontiguousarray(alpha, dtype=np.float32)
     beta = np.ascontiguousarray(beta, dtype=np.float32)
     G = np.ascontiguousarray(G, dtype=np.float32).ravel()
-    if G.size == S:
-        G = np.tile(G, B)          # one G row per pulse (XTAL layout, KN_kernel :222)
-    if G.size != S * B:
-        raise ValueError("G must hold S or S*B values")
+    if variant == 0:
+        if G.size == S:
+            G = np.tile(G, B)      # one G row per pulse (XTAL layout, KN_kernel :222)
+        if G.size != S * B:
+            raise ValueError("G must hold S or S*B values")
+    elif G.size != S:
+        raise ValueError("G must hold S values (one poling shared by the batch)")
     Ap = np.zeros((B, nch, N), np.complex64) if Ap is None else np.ascontiguousarray(Ap, np.complex64).copy()
     sm = np.zeros(S, np.float32) if stepmods is None else np.ascontiguousarray(stepmods, np.float32).copy()
     A = np.zeros((B, N), np.complex64)
@@ -91,7 +104,8 @@ def run(E, alpha, G, beta, *, w0, bdiffw0, h, n_steps, dt, max_err, min_err, sel
     fptr = ctypes.POINTER(ctypes.c_float)
     iptr = ctypes.POINTER(ctypes.c_int)
     rc = lib().refmex_run(
-        CUBIN.encode(), E.view(np.float32).ctypes.data_as(fptr), ctypes.c_int(N), ctypes.c_int(B),
+        HEUN_CUBINS[variant].encode(), ctypes.c_int(variant), E.view(np.float32).ctypes.data_as(fptr),
+        ctypes.c_int(N), ctypes.c_int(B),
         alpha.ctypes.data_as(fptr), G.ctypes.data_as(fptr), beta.ctypes.data_as(fptr),
         ctypes.c_float(w0), ctypes.c_double(bdiffw0), ctypes.c_float(h), ctypes.c_int(S),
         ctypes.c_double(dt), ctypes.c_float(max_err), ctypes.c_float(min_err), ctypes.c_float(sel),

@@ -223,3 +223,45 @@ def test_propagator_rk23_matches_reference_ode23_kernels(refode23, N, cta):
     print(dict(N=N, cta=cta, attempts=st["attempts"], field_err=err))
     assert np.array_equal(sm, ref.stepmods), "stepmods record differs"
     assert err <= FIELD_TOL, err
+
+
+# ---------------------------------------------------------------------------
+# The other Heun MEX files: BATCH_OP (one shared G), NO_BC (unshifted time, no
+# absorber), HARD_BC (unshifted time, zeroing absorber); int sel, truncated chunks
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_heun_variants_match_reference_kernels(oracle, variant):
+    import dataclasses
+    from oracle import ref_mex
+    from optifax_gb300 import _native as nat
+    from tests.test_parity_gpu import _gpu_pass, _oracle_pass
+    ok, why = ref_mex.available(ref_mex.HEUN_CUBINS[variant])
+    if not ok:
+        pytest.skip(why)
+    win, si, E = make_case(N=2048, length=0.2e-3, power=2.0)
+    E64 = np.asarray(E[0], np.complex64).astype(np.complex128)
+    kw = dict(w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps, dt=si.dt,
+              max_err=si.max_err, min_err=si.min_err, sel=si.sel, variant=variant)
+    ref = ref_mex.run(E[0], si.alpha, si.G, si.beta, **kw)
+    dec = ref.trace[:, 2] & 3
+    orc = _oracle_pass(oracle, si, E64, nat.HEUN, variant, forced=dec)
+    own = _oracle_pass(oracle, si, E64, nat.HEUN, variant)
+    assert np.array_equal(orc.trace[0][:, :2], ref.trace[:, :2]), "step schedules differ under replay"
+    same_sched = len(own.trace[0]) == len(ref.trace) and np.array_equal(own.trace[0][:, :2], ref.trace[:, :2])
+    A, Ap, sm, tr, st = _gpu_pass(si, E[0], nat.HEUN, variant, 0, forced=dec)
+    assert st["status"] == 0, st
+    assert np.array_equal(tr[:, :2], ref.trace[:, :2])
+    # FFT-only drift of the reference on the same schedule
+    lin0 = dataclasses.replace(si, G=np.zeros_like(si.G), beta=np.zeros_like(si.beta),
+                               alpha=np.ones_like(si.alpha))
+    rt = ref_mex.run(E[0], lin0.alpha, lin0.G, lin0.beta, forced=dec, **kw)
+    ot = _oracle_pass(oracle, lin0, E64, nat.HEUN, variant, forced=dec)
+    err = rel_l2(ref.A[0], orc.A[0])
+    err_gpu = rel_l2(A, ref.A[0])
+    e_fft = rel_l2(rt.A[0], ot.A[0])
+    print(dict(variant=variant, attempts=ref.attempts, oracle_own_schedule_equal=same_sched,
+               field_err=err, propagator_err=err_gpu, fft_only_err=e_fft))
+    assert np.array_equal(orc.stepmods.astype(np.float32), ref.stepmods)
+    assert np.array_equal(sm, ref.stepmods)
+    assert err <= FIELD_TOL and err_gpu <= FIELD_TOL
+    assert err <= 1.5 * e_fft + 1e-5, "difference larger than the FFT drift explains"
