@@ -9,10 +9,11 @@
  * Parity status: PINNED to the reference's own CUDA kernels.  The reference
  * ships no golden vectors, fixtures or tests for this path, and its MATLAB
  * code cannot run here; its MEX kernels (OPO_CUDA_BATCH_XTAL.cu, _BATCH_OP.cu,
- * _NO_BC.cu, _HARD_BC.cu, ode23/OPO_CUDA_ODE23.cu) are compiled unmodified into cubins and driven with
- * cuFFT by oracle/ref_mex.cpp.  tests/test_reference_kernels_gpu.py checks this
- * restatement against them on the GPU: identical step schedules (Heun), and
- * fields within the drift of cuFFT's FP32 round trips.  Known-answer tests
+ * _NO_BC.cu, _HARD_BC.cu, ode23/OPO_CUDA_ODE23.cu) are compiled unmodified into
+ * cubins and driven with cuFFT by oracle/ref_mex.cpp.
+ * tests/test_reference_kernels_gpu.py checks this restatement against them on
+ * the GPU: identical step schedules (Heun), and fields within the drift of
+ * cuFFT's FP32 round trips.  Known-answer tests
  * (pure dispersion, FFT, convergence order, replay, the reject rules) are in
  * tests/test_oracle.py.  The NEE_CPU.m schedule (MATLAB only) stays unpinned.
  *
