@@ -22,7 +22,8 @@ using namespace ofx;
 
 struct optifax_context {
     int device = 0;
-    std::map<int, Twiddle*> tw;          // n -> n/2 entries, W_n^e
+    std::map<int, Twiddle*> tw;          // N -> W_N^i, i < 64 (cluster exchange)
+    std::map<int, Twiddle*> quadtw;      // M -> W_M^y, y < M/4 (cluster exchange)
     std::map<int, Twiddle*> passtw;      // M -> pass-1 table [16][M/16] then pass-2 [16][M/256]
     PulseDev* d_desc = nullptr;
     size_t desc_cap = 0;
@@ -36,9 +37,12 @@ struct optifax_context {
 
 namespace {
 
-__global__ void twiddle_kernel(Twiddle* out, int n) {
+// out[e] = W_n^e = exp(-2 pi i e / n) for e < count, rounded to FP32, with
+// d = 1/|w|^2 - 1 in FP64.  The cluster exchange's tables: the quarter period of
+// W_M (count M/4) and W_N^i for i < 64.
+__global__ void twiddle_kernel(Twiddle* out, int n, int count) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n / 2) return;
+    if (e >= count) return;
     double s, c;
     sincospi(-2.0 * (double)e / (double)n, &s, &c);
     float cf = (float)c, sf = (float)s;
@@ -73,19 +77,21 @@ int cuda_fail(optifax_context* h, cudaError_t e, const char* what) {
     return fail(h, OPTIFAX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-const Twiddle* get_twiddles(optifax_context* h, int n, cudaStream_t st, int* rc) {
-    auto it = h->tw.find(n);
-    if (it != h->tw.end()) return it->second;
+// W_n^e for e < count, built once per (n, count) map and kept for the context
+const Twiddle* get_table(optifax_context* h, std::map<int, Twiddle*>& cache, int n, int count,
+                         cudaStream_t st, int* rc) {
+    auto it = cache.find(n);
+    if (it != cache.end()) return it->second;
     Twiddle* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, sizeof(Twiddle) * (size_t)(n / 2));
+    cudaError_t e = cudaMalloc(&d, sizeof(Twiddle) * (size_t)count);
     if (e != cudaSuccess) { *rc = cuda_fail(h, e, "cudaMalloc(twiddles)"); return nullptr; }
-    twiddle_kernel<<<(n / 2 + 255) / 256, 256, 0, st>>>(d, n);
+    twiddle_kernel<<<(count + 255) / 256, 256, 0, st>>>(d, n, count);
     e = cudaGetLastError();
     if (e != cudaSuccess) { cudaFree(d); *rc = cuda_fail(h, e, "twiddle_kernel"); return nullptr; }
     // tables are shared by every stream of the context: finish building them now
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { cudaFree(d); *rc = cuda_fail(h, e, "twiddle_kernel sync"); return nullptr; }
-    h->tw[n] = d;
+    cache[n] = d;
     return d;
 }
 
@@ -198,6 +204,14 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
     for (auto& g : groups) {
         std::stable_sort(g.d.begin(), g.d.end(),
                          [](const PulseDev& x, const PulseDev& y) { return pulse_cost(x) > pulse_cost(y); });
+    }
+    // groups in order of their longest pulse, longest first: the block scheduler
+    // serves earlier launches first, so the critical path starts at once (and large
+    // clusters find whole GPCs free only at the start)
+    auto group_key = [](const Group& g) { return g.d.empty() ? 0.0 : pulse_cost(g.d.front()); };
+    std::stable_sort(groups.begin(), groups.end(),
+                     [&](const Group& x, const Group& y) { return group_key(x) > group_key(y); });
+    for (auto& g : groups) {
         n_desc += g.d.size();
         if (g.C > 1) need_xch += g.d.size() * 2 * (size_t)g.M * g.C;
         for (const auto& d : g.d)
@@ -238,13 +252,15 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
     // happen between the launches
     std::vector<FftTables> tabv(groups.size());
     for (size_t gi = 0; gi < groups.size(); ++gi) {
-        const Twiddle* twp = get_pass_twiddles(h, groups[gi].M, st, &rc);
+        const int M = groups[gi].M;
+        const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
         if (!twp) return rc;
-        const Twiddle* twN = get_twiddles(h, groups[gi].M * groups[gi].C, st, &rc);
-        if (!twN) return rc;
         tabv[gi].tw1 = twp;
-        tabv[gi].tw2 = twp + groups[gi].M;
-        tabv[gi].twN = twN;
+        tabv[gi].tw2 = twp + M;
+        tabv[gi].quad = get_table(h, h->quadtw, M, M / 4, st, &rc);       // quarter period of W_M
+        if (!tabv[gi].quad) return rc;
+        tabv[gi].low = get_table(h, h->tw, M * groups[gi].C, 64, st, &rc);  // W_N^i, i < 64
+        if (!tabv[gi].low) return rc;
     }
     if (groups.size() > 1) {
         e = cudaEventRecord(h->ev[0], st);
@@ -393,6 +409,7 @@ int optifax_destroy(optifax_handle h) {
     cudaDeviceSynchronize();
     for (auto& kv : h->tw) cudaFree(kv.second);
     for (auto& kv : h->passtw) cudaFree(kv.second);
+    for (auto& kv : h->quadtw) cudaFree(kv.second);
     if (h->d_desc) cudaFree(h->d_desc);
     if (h->d_grid_flags) cudaFree(h->d_grid_flags);
     if (h->d_xch) cudaFree(h->d_xch);

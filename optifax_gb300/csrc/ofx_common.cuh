@@ -52,6 +52,31 @@ __device__ __forceinline__ float2 tw_inv(float2 v, const Twiddle& w) {
     return make_float2(fmaf(t.x, w.d, t.x), fmaf(t.y, w.d, t.y));
 }
 
+// W_M^x for 0 <= x < M from the quarter-period table q[y] = W_M^y, y < M/4
+// (kept in shared memory): x = k M/4 + y gives W_M^y (-i)^k, a swap and sign
+// changes, so the value and its d are those of a full table.
+template <int M>
+__device__ __forceinline__ Twiddle quad_tw(const Twiddle* q, int x) {
+    const Twiddle w = q[x & (M / 4 - 1)];
+    const int k = (x / (M / 4)) & 3;
+    float c = (k & 1) ? w.s : w.c;
+    float s = (k & 1) ? -w.c : w.s;
+    if (k & 2) { c = -c; s = -s; }
+    return Twiddle{c, s, w.d, 0.f};
+}
+
+// 1/|w|^2 - 1 for a computed |w| ~ 1.  g = |w|^2 - 1 is formed without
+// rounding error beyond the last add (products split by fma; the subtractions
+// are exact by Sterbenz's lemma), then 1/(1 + g) - 1 = -g + g^2 (g ~ 1e-7).
+__device__ __forceinline__ float inv_norm2_m1(float2 w) {
+    const float p1 = w.x * w.x, p2 = w.y * w.y;
+    const float e1 = fmaf(w.x, w.x, -p1), e2 = fmaf(w.y, w.y, -p2);
+    const float big = fmaxf(p1, p2), small = fminf(p1, p2);
+    const float g0 = (big >= 0.5f) ? (big - 1.0f) + small : (p1 - 0.5f) + (p2 - 0.5f);
+    const float g = g0 + (e1 + e2);
+    return fmaf(g, g, -g);
+}
+
 __device__ __forceinline__ int bitrev(int x, int bits) {
     return bits == 0 ? 0 : (int)(__brev((unsigned)x) >> (32 - bits));
 }

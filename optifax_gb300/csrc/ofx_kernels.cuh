@@ -13,7 +13,7 @@ struct KernelEntry { KernelFn fn; size_t smem; int M, C, method; };
 
 template <int M, int C, int METH>
 KernelEntry kernel_entry() {
-    return KernelEntry{&pass_kernel<M, C, METH>, Smem<M, METH>::bytes, M, C, METH};
+    return KernelEntry{&pass_kernel<M, C, METH>, Smem<M, METH, C>::bytes, M, C, METH};
 }
 
 void register_kernels_heun_large(std::vector<KernelEntry>& v);

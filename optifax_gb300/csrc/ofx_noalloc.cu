@@ -36,11 +36,13 @@ constexpr int kM = 4096;                 // points per CTA
 constexpr int kMaxN = 16384;             // cluster of 4
 constexpr size_t kDescBytes = 512;
 constexpr size_t kPassTw = kM + 16 * (kM / 256);          // pass-1 + pass-2 outer twiddles
-constexpr size_t kNTw = kMaxN / 2;                         // W_N^e, e < N/2
+constexpr size_t kQuadTw = kM / 4;                         // W_M^y, y < M/4 (cluster exchange)
+constexpr size_t kLowTw = 64;                              // W_N^i, i < 64 (cluster exchange)
 constexpr size_t kXch = 2 * (size_t)kMaxN;                 // exchange buffer (complex)
 constexpr size_t kOffPass = kDescBytes;
-constexpr size_t kOffN = kOffPass + sizeof(Twiddle) * kPassTw;
-constexpr size_t kOffXch = kOffN + sizeof(Twiddle) * kNTw;
+constexpr size_t kOffQuad = kOffPass + sizeof(Twiddle) * kPassTw;
+constexpr size_t kOffN = kOffQuad + sizeof(Twiddle) * kQuadTw;
+constexpr size_t kOffXch = kOffN + sizeof(Twiddle) * kLowTw;
 constexpr size_t kBytes = kOffXch + sizeof(float2) * kXch;
 static_assert(sizeof(PulseDev) <= kDescBytes, "descriptor slot too small");
 
@@ -66,9 +68,10 @@ __global__ void noalloc_pass_twiddles(Twiddle* out, int L) {
     out[idx] = Twiddle{cf, sf, (float)(1.0 / m2 - 1.0), 0.f};
 }
 
-__global__ void noalloc_n_twiddles(Twiddle* out, int n) {
+// out[e] = W_n^e for e < count (FP32, d = 1/|w|^2 - 1 in FP64)
+__global__ void noalloc_twiddles(Twiddle* out, int n, int count) {
     int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n / 2) return;
+    if (e >= count) return;
     double s, c;
     sincospi(-2.0 * (double)e / (double)n, &s, &c);
     float cf = (float)c, sf = (float)s;
@@ -133,11 +136,13 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
             Twiddle* tw = reinterpret_cast<Twiddle*>(base + kOffPass);
             noalloc_pass_twiddles<<<(kM + 255) / 256, 256, 0, st>>>(tw, kM);
             noalloc_pass_twiddles<<<1, 256, 0, st>>>(tw + kM, kM / 16);
+            noalloc_twiddles<<<(int)((kQuadTw + 255) / 256), 256, 0, st>>>(
+                reinterpret_cast<Twiddle*>(base + kOffQuad), kM, (int)kQuadTw);
             if (cudaGetLastError() != cudaSuccess) return OPTIFAX_ERR_CUDA;
             ds.pass_tables = true;
         }
         if (ds.n_table != N) {
-            noalloc_n_twiddles<<<(N / 2 + 255) / 256, 256, 0, st>>>(reinterpret_cast<Twiddle*>(base + kOffN), N);
+            noalloc_twiddles<<<1, 64, 0, st>>>(reinterpret_cast<Twiddle*>(base + kOffN), N, (int)kLowTw);
             if (cudaGetLastError() != cudaSuccess) return OPTIFAX_ERR_CUDA;
             ds.n_table = N;
         }
@@ -189,7 +194,8 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
     FftTables tabs;
     tabs.tw1 = reinterpret_cast<const Twiddle*>(base + kOffPass);
     tabs.tw2 = tabs.tw1 + kM;
-    tabs.twN = reinterpret_cast<const Twiddle*>(base + kOffN);
+    tabs.quad = reinterpret_cast<const Twiddle*>(base + kOffQuad);
+    tabs.low = reinterpret_cast<const Twiddle*>(base + kOffN);
     cudaLaunchConfig_t lc;
     memset(&lc, 0, sizeof(lc));
     lc.gridDim = dim3((unsigned)C, 1, 1);

@@ -74,7 +74,9 @@ struct PulseDev {
 struct FftTables {
     const Twiddle* tw1;      // pass-1 outer twiddles [16][M/16]: W_M^{off r}
     const Twiddle* tw2;      // pass-2 outer twiddles [16][M/256]: W_{M/16}^{off r}
-    const Twiddle* twN;      // W_N^e, e in [0, N/2): cluster exchange
+    // cluster exchange (copied to shared memory): W_N^e = W_M^{(64/C)(e >> 6)} W_N^{e & 63}
+    const Twiddle* quad;     // W_M^y, y in [0, M/4)
+    const Twiddle* low;      // W_N^i, i in [0, 64)
 };
 
 struct KernelCfg {
@@ -211,7 +213,7 @@ __device__ __forceinline__ float2 zphase(uint64_t tau_z4, float pos) {
 // ---------------------------------------------------------------------------
 // shared-memory layout
 // ---------------------------------------------------------------------------
-template <int M, int METHOD>
+template <int M, int METHOD, int C>
 struct Smem {
     static constexpr int T = M / 16;
     static constexpr int PADM = M + M / 16;
@@ -228,7 +230,11 @@ struct Smem {
     static constexpr size_t off_edge = off_dfc + sizeof(int) * NCACHE;
     static constexpr size_t off_red = off_edge + sizeof(float2) * 4 * T;
     static constexpr size_t off_dred = off_red + 256;               // FP64 reduction slots
-    static constexpr size_t bytes = off_dred + sizeof(double) * (8 * 4 + 2 * 16 * 4 + 4);
+    // exchange twiddle tables (16-byte entries, clusters only): quarter-period W_M,
+    // W_N^i for i < 64
+    static constexpr size_t off_quad = (off_dred + sizeof(double) * (8 * 4 + 2 * 16 * 4 + 4) + 15) & ~size_t(15);
+    static constexpr size_t off_low = off_quad + (C > 1 ? sizeof(Twiddle) * (M / 4) : 0);
+    static constexpr size_t bytes = off_low + (C > 1 ? sizeof(Twiddle) * 64 : 0);
 };
 
 // ---------------------------------------------------------------------------
@@ -262,14 +268,27 @@ __device__ __forceinline__ void exchange_edges(float2* edge, int& par, int t, in
     par ^= 1;
 }
 
-// N-point twiddle W_N^e for e in [0, N) from a half table
-__device__ __forceinline__ float2 twn_fwd(float2 v, const Twiddle* __restrict__ tw, int e, int half) {
-    if (e >= half) { float2 r = tw_fwd(v, tw[e - half]); return make_float2(-r.x, -r.y); }
-    return tw_fwd(v, tw[e]);
+// N-point twiddle W_N^e, 0 <= e < N = C M, from the two shared-memory tables:
+// W_M^{(64/C)(e >> 6)} (quarter table, exact) times W_N^{e & 63}.  The product is
+// rounded once; the inverse multiplies by its exact reciprocal conj(w)(1 + d),
+// d = 1/|w|^2 - 1 formed from w itself, so forward + inverse carry no gain.
+template <int M, int C>
+__device__ __forceinline__ float2 twn_val(const Twiddle* quad, const Twiddle* low, int e) {
+    static_assert(64 % C == 0, "cluster size must divide 64");
+    const Twiddle a = quad_tw<M>(quad, (64 / C) * (e >> 6));
+    const Twiddle b = low[e & 63];
+    return cmul(make_float2(a.c, a.s), make_float2(b.c, b.s));
 }
-__device__ __forceinline__ float2 twn_inv(float2 v, const Twiddle* __restrict__ tw, int e, int half) {
-    if (e >= half) { float2 r = tw_inv(v, tw[e - half]); return make_float2(-r.x, -r.y); }
-    return tw_inv(v, tw[e]);
+template <int M, int C>
+__device__ __forceinline__ float2 twn_fwd(float2 v, const Twiddle* quad, const Twiddle* low, int e) {
+    return cmul(v, twn_val<M, C>(quad, low, e));
+}
+template <int M, int C>
+__device__ __forceinline__ float2 twn_inv(float2 v, const Twiddle* quad, const Twiddle* low, int e) {
+    const float2 w = twn_val<M, C>(quad, low, e);
+    const float2 t = cmulc(v, w);
+    const float d = inv_norm2_m1(w);
+    return make_float2(fmaf(t.x, d, t.x), fmaf(t.y, d, t.y));
 }
 
 // Four-step split of the N = C M transform through global memory (L2):
@@ -281,9 +300,9 @@ __device__ __forceinline__ float2 twn_inv(float2 v, const Twiddle* __restrict__ 
 // at cluster scope covers global memory); loads and stores bypass L1.
 template <int M, int C>
 __device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx, float2* __restrict__ yy,
-                                                   const Twiddle* __restrict__ twN, int t, int c) {
+                                                   const Twiddle* quad, const Twiddle* low, int t, int c) {
     if constexpr (C > 1) {
-        constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
+        constexpr int T = M / 16, PER = 16 / C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
         float2 v[PER][C];
 #pragma unroll
         for (int u = 0; u < PER; ++u)          // every load in flight before any use
@@ -292,11 +311,11 @@ __device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
             int n2 = c * (M / C) + t + T * u;
-            dif_stages<N, C, C>(v[u], 0, twN);
+            dft_dif<C>(v[u]);
 #pragma unroll
             for (int r = 0; r < C; ++r) {
                 int k1 = bitrev(r, LOGC);
-                __stcg(yy + k1 * M + n2, twn_fwd(v[u][r], twN, n2 * k1, N / 2));
+                __stcg(yy + k1 * M + n2, k1 == 0 ? v[u][r] : twn_fwd<M, C>(v[u][r], quad, low, n2 * k1));
             }
         }
     }
@@ -304,9 +323,10 @@ __device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx
 
 template <int M, int C>
 __device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy, float2* __restrict__ xx,
-                                                   const Twiddle* __restrict__ twN, int t, int c, float invN) {
+                                                   const Twiddle* quad, const Twiddle* low, int t, int c,
+                                                   float invN) {
     if constexpr (C > 1) {
-        constexpr int T = M / 16, PER = 16 / C, N = M * C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
+        constexpr int T = M / 16, PER = 16 / C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
         float2 v[PER][C];
 #pragma unroll
         for (int u = 0; u < PER; ++u)          // every load in flight before any use
@@ -316,8 +336,8 @@ __device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy
         for (int u = 0; u < PER; ++u) {
             int n2 = c * (M / C) + t + T * u;
 #pragma unroll
-            for (int r = 0; r < C; ++r) v[u][r] = twn_inv(v[u][r], twN, n2 * bitrev(r, LOGC), N / 2);
-            dit_stages<N, C, C>(v[u], 0, twN);
+            for (int r = 1; r < C; ++r) v[u][r] = twn_inv<M, C>(v[u][r], quad, low, n2 * bitrev(r, LOGC));
+            dft_dit_inv<C>(v[u]);
 #pragma unroll
             for (int n1 = 0; n1 < C; ++n1) __stcg(xx + n1 * M + n2, cscale(v[u][n1], invN));
         }
@@ -412,7 +432,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
     constexpr int T = M / 16;
     constexpr int N = M * C;
     constexpr int LOG2M = FftShape<M>::LOG2M;
-    using SM = Smem<M, METHOD>;
+    using SM = Smem<M, METHOD, C>;
     extern __shared__ __align__(16) unsigned char smem[];
     float2* bufE = reinterpret_cast<float2*>(smem + SM::off_buf);
     float2* bufX = bufE + SM::PADM;
@@ -425,7 +445,8 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
     int* dfc_s = reinterpret_cast<int*>(smem + SM::off_dfc);
     const Twiddle* __restrict__ tw1 = tabs.tw1;
     const Twiddle* __restrict__ tw2 = tabs.tw2;
-    const Twiddle* __restrict__ twN = tabs.twN;
+    Twiddle* quad_s = reinterpret_cast<Twiddle*>(smem + SM::off_quad);
+    Twiddle* low_s = reinterpret_cast<Twiddle*>(smem + SM::off_low);
     float2* edge = reinterpret_cast<float2*>(smem + SM::off_edge);
     int* red = reinterpret_cast<int*>(smem + SM::off_red);
     double* dred = reinterpret_cast<double*>(smem + SM::off_dred);
@@ -443,6 +464,10 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
 
     // ---- prologue -------------------------------------------------------
     for (int i = t; i < 64; i += T) red[i] = 0;
+    if constexpr (C > 1) {
+        for (int i = t; i < M / 4; i += T) quad_s[i] = tabs.quad[i];
+        for (int i = t; i < 64; i += T) low_s[i] = tabs.low[i];
+    }
     float2 cph[16], a[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
@@ -665,7 +690,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     float2* fbuf = (C > 1) ? bufX : bufE;
                     float2* ybuf = (C > 1) ? P.xch + N + c * M : nullptr;
                     if constexpr (C > 1) {
-                        exchange_forward_g<M, C>(P.xch, P.xch + N, twN, t, c);
+                        exchange_forward_g<M, C>(P.xch, P.xch + N, quad_s, low_s, t, c);
                         cg::this_cluster().sync();
                     } else {
                         __syncthreads();
@@ -753,7 +778,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     fft_inverse_from_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     if constexpr (C > 1) {
                         cg::this_cluster().sync();
-                        exchange_inverse_g<M, C>(P.xch + N, P.xch, twN, t, c, invN);
+                        exchange_inverse_g<M, C>(P.xch + N, P.xch, quad_s, low_s, t, c, invN);
                         cg::this_cluster().sync();
                         const float4* src = reinterpret_cast<const float4*>(P.xch + c * M + 16 * t);
 #pragma unroll
