@@ -291,15 +291,22 @@ __device__ __forceinline__ float2 twn_inv(float2 v, const Twiddle* quad, const T
     return make_float2(fmaf(t.x, d, t.x), fmaf(t.y, d, t.y));
 }
 
-// Four-step split of the N = C M transform through global memory (L2):
-// forward step 1 (C-point DFTs over CTAs, twiddle W_N^{n2 k1}).  L2 moves the
-// field between the CTAs of a cluster far faster than distributed shared
-// memory: each CTA reads C slices of the other blocks, computes the C-point
-// DFTs of its n2 slice and writes the results to their owners' blocks.
-// Ordering comes from the cluster barriers around the calls (release/acquire
-// at cluster scope covers global memory); loads and stores bypass L1.
+// Exchange results go straight into their owners' shared memory for clusters of
+// up to 8 CTAs; 16-CTA clusters keep them in global memory (L2), where their
+// wider fan-out measured faster (and the kernel stays free of spills).
+template <int C>
+constexpr bool kPushExchange = (C <= 8);
+
+// Four-step split of the N = C M transform: forward step 1 (C-point DFTs over
+// CTAs, twiddle W_N^{n2 k1}).  Each CTA gathers its n2 slice of the C blocks
+// from global memory (L2; many loads in flight, far faster than pulling through
+// distributed shared memory), computes the C-point DFTs and stores the results
+// in their owners' shared memory (`buf`, the owner's FFT buffer, at phys(n2))
+// or, for 16-CTA clusters, in their blocks of `yy` (global).  Ordering comes
+// from the cluster barriers around the calls (release/acquire at cluster scope
+// covers global and distributed shared memory); global accesses bypass L1.
 template <int M, int C>
-__device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx, float2* __restrict__ yy,
+__device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx, float2* buf, float2* yy,
                                                    const Twiddle* quad, const Twiddle* low, int t, int c) {
     if constexpr (C > 1) {
         constexpr int T = M / 16, PER = 16 / C, LOGC = (C == 2) ? 1 : (C == 4) ? 2 : (C == 8) ? 3 : 4;
@@ -315,14 +322,20 @@ __device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx
 #pragma unroll
             for (int r = 0; r < C; ++r) {
                 int k1 = bitrev(r, LOGC);
-                __stcg(yy + k1 * M + n2, k1 == 0 ? v[u][r] : twn_fwd<M, C>(v[u][r], quad, low, n2 * k1));
+                const float2 y = k1 == 0 ? v[u][r] : twn_fwd<M, C>(v[u][r], quad, low, n2 * k1);
+                if constexpr (kPushExchange<C>) remote<C>(buf, k1)[phys(n2)] = y;
+                else __stcg(yy + k1 * M + n2, y);
             }
         }
     }
 }
 
+// Inverse step: gather the n2 slice of the C inverse-transformed blocks from
+// global memory, undo the twiddles, C-point inverse DFTs, scale by 1/N and store
+// each result in its owner's shared memory (`buf` at phys(n2)) or, for 16-CTA
+// clusters, in its block of `xx` (global).
 template <int M, int C>
-__device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy, float2* __restrict__ xx,
+__device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy, float2* buf, float2* xx,
                                                    const Twiddle* quad, const Twiddle* low, int t, int c,
                                                    float invN) {
     if constexpr (C > 1) {
@@ -339,7 +352,10 @@ __device__ __forceinline__ void exchange_inverse_g(const float2* __restrict__ yy
             for (int r = 1; r < C; ++r) v[u][r] = twn_inv<M, C>(v[u][r], quad, low, n2 * bitrev(r, LOGC));
             dft_dit_inv<C>(v[u]);
 #pragma unroll
-            for (int n1 = 0; n1 < C; ++n1) __stcg(xx + n1 * M + n2, cscale(v[u][n1], invN));
+            for (int n1 = 0; n1 < C; ++n1) {
+                if constexpr (kPushExchange<C>) remote<C>(buf, n1)[phys(n2)] = cscale(v[u][n1], invN);
+                else __stcg(xx + n1 * M + n2, cscale(v[u][n1], invN));
+            }
         }
     }
 }
@@ -687,10 +703,12 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     // D = alpha^s exp(-i beta s): transform rounding then scales with
                     // |D - 1| instead of |E|.  At the end of an OPO pass the full
                     // spectrum goes through the cavity instead: A_new = IFFT(D FFT(E) fb + pump) / N.
+                    // clusters: the exchanged block lands in bufX (the FFT buffer; bufE keeps E),
+                    // or in ybuf (global) for 16-CTA clusters
                     float2* fbuf = (C > 1) ? bufX : bufE;
                     float2* ybuf = (C > 1) ? P.xch + N + c * M : nullptr;
                     if constexpr (C > 1) {
-                        exchange_forward_g<M, C>(P.xch, P.xch + N, quad_s, low_s, t, c);
+                        exchange_forward_g<M, C>(P.xch, bufX, P.xch + N, quad_s, low_s, t, c);
                         cg::this_cluster().sync();
                     } else {
                         __syncthreads();
@@ -710,7 +728,7 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                         }
                     }
                     float2 v[16];
-                    fft_forward_to_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
+                    fft_forward_to_regs<M>(fbuf, tw1, tw2, t, v, kPushExchange<C> ? nullptr : ybuf);
                     float2* apc = (last_in_chunk && P.Ap) ? P.Ap + (size_t)chunk * N : nullptr;
                     float part[4] = {0.f, 0.f, 0.f, 0.f};
                     // the trip's crystal output goes to the cavity scratch; the cavity
@@ -778,15 +796,23 @@ pass_kernel(const PulseDev* __restrict__ pulses, FftTables tabs, KernelCfg cfg) 
                     fft_inverse_from_regs<M>(fbuf, tw1, tw2, t, v, ybuf);
                     if constexpr (C > 1) {
                         cg::this_cluster().sync();
-                        exchange_inverse_g<M, C>(P.xch + N, P.xch, quad_s, low_s, t, c, invN);
+                        exchange_inverse_g<M, C>(P.xch + N, bufX, P.xch, quad_s, low_s, t, c, invN);
                         cg::this_cluster().sync();
-                        const float4* src = reinterpret_cast<const float4*>(P.xch + c * M + 16 * t);
+                        if constexpr (kPushExchange<C>) {
 #pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            float4 w = __ldcg(src + j);
-                            float2 d0 = make_float2(w.x, w.y), d1 = make_float2(w.z, w.w);
-                            a[2 * j] = cav ? d0 : cadd(bufE[phys(16 * t + 2 * j)], d0);
-                            a[2 * j + 1] = cav ? d1 : cadd(bufE[phys(16 * t + 2 * j + 1)], d1);
+                            for (int j = 0; j < 16; ++j) {
+                                const float2 d = bufX[phys(16 * t + j)];
+                                a[j] = cav ? d : cadd(bufE[phys(16 * t + j)], d);
+                            }
+                        } else {
+                            const float4* src = reinterpret_cast<const float4*>(P.xch + c * M + 16 * t);
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                float4 w = __ldcg(src + j);
+                                float2 d0 = make_float2(w.x, w.y), d1 = make_float2(w.z, w.w);
+                                a[2 * j] = cav ? d0 : cadd(bufE[phys(16 * t + 2 * j)], d0);
+                                a[2 * j + 1] = cav ? d1 : cadd(bufE[phys(16 * t + 2 * j + 1)], d1);
+                            }
                         }
                     } else {
                         if (cav) {
