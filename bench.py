@@ -31,8 +31,8 @@ WORKLOAD = ("SPOPO round trips: N=2^14 over 12 ps, 5 mm MgO:PPLN 30 um, sech2 10
 
 
 # DRAM bytes per OPO round trip of pass_kernel<4096, 4, HEUN>: ncu dram__bytes_read.sum
-# (2,148,096) + dram__bytes_write.sum (206,336) of the bench's timed 10-trip launch
-TRAFFIC_PER_TRIP = (2148096 + 206336) / 10.0
+# (1,914,112) + dram__bytes_write.sum (159,232) of the bench's timed 10-trip launch
+TRAFFIC_PER_TRIP = (1914112 + 159232) / 10.0
 
 
 def _spec():
@@ -457,7 +457,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": TRAFFIC_PER_TRIP * K,
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the timed "
-                                           "launch at 10 trips (2.35 MB), per trip x trips: the field stays "
+                                           "launch at 10 trips (2.07 MB), per trip x trips: the field stays "
                                            "on chip, so real DRAM traffic is tables and per-step G reads",
                          "peak_kind": peak_kind,
                          "algorithmic": "16 B per grid point per step attempt",
