@@ -128,6 +128,47 @@ def cpu_oracle_sample(spec, fraction=0.05, threads=1, field=None, attempts_per_t
                       f"({att} attempts, {el:.1f} s), {how}"}
 
 
+def cpu_sweep_sample(insts, gpu_stats, cores, n_sample=16, fraction=0.02):
+    """FP64 C oracle on a bounded sample of the sweep: the first `fraction` of the
+    steps of `n_sample` instances spread over the list.  Cost per unit of
+    attempts x N log2 N, measured on one core (serially) and on `cores` threads
+    (instances side by side; the oracle releases the GIL), scaled to the whole
+    sweep by the GPU's own attempt counts."""
+    import concurrent.futures as cf
+    import math
+    import numpy as np
+    from oracle import oracle as orc
+    from optifax_gb300 import sweep
+    step = max(1, len(insts) // n_sample)
+    jobs = []
+    for i in list(range(0, len(insts), step))[:n_sample]:
+        win, si, e = sweep.build_inputs(insts[i])
+        S = max(8, int(si.n_steps * fraction))
+        jobs.append((si, e, S, float(np.ceil(S / 4))))
+
+    def one(job):
+        si, e, S, sel = job
+        r = orc.run(e, si.alpha, si.G[:S], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=S,
+                    dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=sel, nthreads=1)
+        n = e.shape[-1]
+        return r.stats[0]["attempts"] * n * math.log2(n)
+
+    t0 = time.perf_counter()
+    work = sum(one(j) for j in jobs)
+    t_one = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(one, jobs))
+    t_all = time.perf_counter() - t0
+    total = sum(st["attempts"] * i.n_points * math.log2(i.n_points) for st, i in zip(gpu_stats, insts))
+    est_one, est_all = t_one / work * total, t_all / work * total
+    return {"value": len(insts) / est_all, "unit": "passes/s", "cores": cores, "kind": "port",
+            "single_core": len(insts) / est_one,
+            "sample": f"FP64 C oracle, first {fraction:.0%} of the steps of {len(jobs)} of the {len(insts)} "
+                      f"instances ({t_one:.1f} s on 1 core, {t_all:.1f} s on {cores} threads), scaled to the "
+                      f"sweep by attempts x N log2 N with the GPU's attempt counts"}
+
+
 def reference_gpu_sample(spec, fraction=0.1):
     """The reference's own CUDA kernels (OPO_CUDA_BATCH_XTAL.cu compiled unmodified,
     driven with cuFFT as its MEX driver does) on the first `fraction` of one crystal
@@ -318,6 +359,8 @@ def run_sweep(args):
                          "algorithmic": "16 B per grid point per step attempt"},
             "gpu_launches": len({(i.n_points) for i in insts}),
             "clocks": clk.summary()}
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sweep_sample(insts, stats, os.cpu_count() or 1)
     print(json.dumps(line))
 
 
