@@ -292,6 +292,70 @@ def fno_case(batch: int, reps: int = 3):
                           "gemm_tflops_over_step": flops / (ms / 1e3) / 1e12, "tc_error": tc_error()}))
 
 
+def run_gnlse(args):
+    """chi(3) fibre (gnlsefib.m) power scan: 152 pulses (one per SM), 4096 points over
+    6 ps, sech pulses of 28.4 fs at 835 nm with 1-10 kW peak power, 15 cm of fibre
+    (beta2..beta4, gamma 0.11 /W/m, fR 0.18, self-steepening), 11 saves, RelTol 1e-5.
+    A step is one batch; value = propagations per second."""
+    import math
+    import numpy as np
+    import torch
+    from optifax_gb300 import gnlse
+    torch.cuda.set_device(0)
+    n, window, nb, L, nsaves = 4096, 6e-12, 152, 0.15, 11
+    T = np.arange(-n // 2, n // 2) * (window / n)
+    w0 = 2 * np.pi * 299792458.0 / 835e-9
+    betas = [-1.183e-26, 8.1e-41, -9.5e-56]
+    ops = gnlse.fibre_operators(T, w0, 0.11, betas, 0.0, 0.18, gnlse.raman_response(T))
+    powers = np.linspace(1e3, 1e4, nb)
+    A = np.stack([np.sqrt(p) / np.cosh(T / 28.4e-15) for p in powers]).astype(np.complex64)
+    A_d = torch.from_numpy(A).cuda()
+    for _ in range(max(1, args.warmup)):
+        r = gnlse.propagate(ops, A_d, L, nsaves, w0=w0)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record()
+            r = gnlse.propagate(ops, A_d, L, nsaves, w0=w0)
+            ev1.record()
+            torch.cuda.synchronize()
+            times.append(ev0.elapsed_time(ev1) / 1000.0)
+    t = float(np.mean(times))
+    att = [s_["attempts"] for s_ in r.stats]
+    rhs_evals = 6 * sum(att) + nb
+    flops = rhs_evals * (4 * 5 * n * math.log2(n) + 40 * n)
+    peak, peak_kind = _peaks()
+    achieved = 16.0 * n * rhs_evals / t / 1e9
+    line = {"metric": "chi(3) fibre propagations/s (GNLSE power scan)", "value": nb / t, "unit": "propagations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": t * 1000.0,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"GNLSE power scan: {nb} pulses x {n} points over 6 ps, 28.4 fs sech at 835 nm, "
+                                   "1-10 kW, 15 cm, beta2..beta4, gamma 0.11/W/m, fR 0.18, shock, 11 saves, "
+                                   "RelTol 1e-5", "attempts_min": min(att), "attempts_max": max(att),
+                       "attempts_total": sum(att), "status": sorted({s_["status"] for s_ in r.stats})},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_kind": peak_kind,
+                         "algorithmic": "16 B per grid point per right-hand-side evaluation",
+                         "compute_tflops": flops / t / 1e12},
+            "gpu_launches": 1, "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        from oracle import gnlse_oracle as go
+        o = go.gnlse_ops(T, w0, 0.11, betas, 0.0, 0.18, go.raman_response(T))
+        sample = [0, nb // 2, nb - 1]
+        t0 = time.perf_counter()
+        n_att = sum(go.propagate(o, A[i].astype(np.complex128), L, nsaves).attempts for i in sample)
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nb / (el / n_att * sum(att)), "unit": "propagations/s", "cores": 1,
+                                "kind": "port",
+                                "sample": f"FP64 numpy oracle, full propagation of the 1, 5.5 and 10 kW pulses "
+                                          f"({n_att} attempts, {el:.1f} s), scaled by the GPU's attempt count "
+                                          f"of the batch"}
+    print(json.dumps(line))
+
+
 def run_sweep(args):
     """Config 3: a batch of crystal passes with uneven grids (2^12..2^16), crystals
     (0.5-10 mm, 28-32 um), pumps (0.5-3 W, 100-300 fs), seed 2, in one call.
@@ -372,8 +436,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cta-points", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="opo", choices=["opo", "sweep"],
-                    help="opo: 2^14-point SPOPO round trips (default line); sweep: 256 uneven batched passes")
+    ap.add_argument("--workload", default="opo", choices=["opo", "sweep", "gnlse"],
+                    help="opo: 2^14-point SPOPO round trips (default line); sweep: 256 uneven batched passes; "
+                         "gnlse: chi(3) fibre power scan (152 pulses)")
     ap.add_argument("--sweep-size", type=int, default=256)
     ap.add_argument("--fp64-trips", type=int, default=1,
                     help="round trips of the plain FP64 solver timed beside the line (0: skip)")
@@ -393,6 +458,8 @@ def main():
         return run_reference(args)
     if args.workload == "sweep":
         return run_sweep(args)
+    if args.workload == "gnlse":
+        return run_gnlse(args)
 
     import numpy as np
     import torch

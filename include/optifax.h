@@ -364,6 +364,46 @@ int64_t optifax_setup_work_bytes(int32_t max_points);
 int optifax_setup_pulses(const optifax_setup* s, int32_t n, void* work, int64_t work_bytes,
                          void* stream);
 
+/*
+ * chi(3) fibre GNLSE (replaces toolbox/lib/internal/main/gnlsefib.m:1-89; its caller
+ * is gnlsefibsim.m:30).  The interaction-picture spectral field AW obeys
+ * gnlsefib.m:54-66: dAW/dz = i gamma W ifft(AT ((1 - fR)|AT|^2 + RS)) e^{-Lz},
+ * AT = fft(AW e^{Lz}), RS = dT fR fft(ifft(|AT|^2) RW), L = iB - alpha/2 (MATLAB
+ * fft/ifft conventions), from AW(0) = ifft(A) over [0, length], saved at
+ * linspace(0, length, n_saves).  Integrated by an adaptive Dormand-Prince 5(4) pair
+ * (FSAL) with the tolerances gnlsefib.m passes to ode45 (rtol, atol; NormControl
+ * error norm), steps landing on the save points, positions in units of
+ * length / 2^40.  One CTA per pulse; n_points a power of two in 512..4096.
+ * Per pulse (all DEVICE pointers; arrays in FFT order unless stated):
+ *   A       input field, natural time order (n complex64, sqrt(W))
+ *   B       dispersion sum_m beta_m V^m / m! (n doubles, rad/m)
+ *   W       V + w0 with a shock term, else ones (n floats)
+ *   RW      n ifft(fftshift(hR)) (n complex64), NULL without Raman (or fR = 0)
+ *   gamma   gamma / w0 with a shock term, else gamma; fr, dT, alpha (field loss), length
+ *   AT_out  n_saves x n complex64: time-domain field at each save (natural order)
+ *   AW_out  n_saves x n complex64: fftshift(AW e^{Lz}) dT n at each save (gnlsefib.m:82-89)
+ *   trace   optional: 2 int64 per attempt (step in length/2^40 units, accepted)
+ *   stats   optional: attempts, accepted, status (OPTIFAX_PULSE_* bits)
+ * All pulses of one call share n_points and n_saves.
+ */
+typedef struct {
+    int32_t attempts, accepted, status, reserved;
+} optifax_gnlse_stats;
+typedef struct {
+    int32_t n_points, n_saves;
+    const void* A;
+    const double* B;
+    const float* W;
+    const void* RW;
+    double gamma, fr, dT, alpha, length, rtol, atol;
+    void* AT_out;
+    void* AW_out;
+    int64_t* trace;
+    int32_t trace_cap, max_attempts;
+    optifax_gnlse_stats* stats;
+} optifax_gnlse_pulse;
+int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses, int32_t n_pulses, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,8 @@ EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifa
            "optifax_fno_param_count", "optifax_fno_create", "optifax_fno_destroy", "optifax_fno_set_params",
            "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
            "optifax_ff_encode", "optifax_ff_step",
-           "optifax_ff_encode_env", "optifax_ff_decode_env", "optifax_setup_work_bytes", "optifax_setup_pulses"]
+           "optifax_ff_encode_env", "optifax_ff_decode_env", "optifax_setup_work_bytes", "optifax_setup_pulses",
+           "optifax_gnlse"]
 
 _lib = None
 
@@ -116,6 +117,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_setup_work_bytes.restype = ctypes.c_int64
     lib.optifax_setup_pulses.argtypes = [ctypes.POINTER(OptifaxSetup), i32, vp, i64, vp]
     lib.optifax_setup_pulses.restype = ctypes.c_int
+    lib.optifax_gnlse.argtypes = [vp, ctypes.POINTER(OptifaxGnlsePulse), i32, vp]
+    lib.optifax_gnlse.restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -130,6 +133,21 @@ class OptifaxSetup(ctypes.Structure):
                 ("lambda_lo_nm", ctypes.c_double), ("lambda_hi_nm", ctypes.c_double),
                 ("alpha", ctypes.c_void_p), ("beta", ctypes.c_void_p), ("G", ctypes.c_void_p),
                 ("E", ctypes.c_void_p)]
+
+
+class OptifaxGnlseStats(ctypes.Structure):
+    _fields_ = [("attempts", ctypes.c_int32), ("accepted", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class OptifaxGnlsePulse(ctypes.Structure):
+    _fields_ = [("n_points", ctypes.c_int32), ("n_saves", ctypes.c_int32),
+                ("A", ctypes.c_void_p), ("B", ctypes.c_void_p), ("W", ctypes.c_void_p), ("RW", ctypes.c_void_p),
+                ("gamma", ctypes.c_double), ("fr", ctypes.c_double), ("dT", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("length", ctypes.c_double), ("rtol", ctypes.c_double),
+                ("atol", ctypes.c_double), ("AT_out", ctypes.c_void_p), ("AW_out", ctypes.c_void_p),
+                ("trace", ctypes.c_void_p), ("trace_cap", ctypes.c_int32), ("max_attempts", ctypes.c_int32),
+                ("stats", ctypes.c_void_p)]
 
 
 class OptifaxError(RuntimeError):

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "liboptifax.so")
-SOURCES = ["ofx_api.cu", "ofx_k_heun_large.cu", "ofx_k_heun_small.cu", "ofx_k_rk23.cu", "ofx_k_heun_nee.cu", "ofx_noalloc.cu", "ofx_fp64.cu", "ofx_gemm.cu", "ofx_fno.cu", "ofx_setup.cu"]
+SOURCES = ["ofx_api.cu", "ofx_k_heun_large.cu", "ofx_k_heun_small.cu", "ofx_k_rk23.cu", "ofx_k_heun_nee.cu", "ofx_noalloc.cu", "ofx_fp64.cu", "ofx_gemm.cu", "ofx_fno.cu", "ofx_setup.cu", "ofx_gnlse.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I" + os.path.join(HERE, "..", "include")]

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "ofx_kernels.cuh"
+#include "ofx_gnlse.cuh"
 #include "../../include/optifax.h"
 
 using namespace ofx;
@@ -32,6 +33,10 @@ struct optifax_context {
     std::vector<cudaStream_t> side;      // streams for concurrent launch groups
     std::vector<cudaEvent_t> ev;         // fork/join events
     int* d_grid_flags = nullptr;
+    ofx::GnlseDev* d_gnlse_desc = nullptr;   // GNLSE: descriptors and stage scratch
+    size_t gnlse_desc_cap = 0;
+    float2* d_gnlse_k = nullptr;
+    size_t gnlse_k_cap = 0;                  // complex values
     std::string last_error;
 };
 
@@ -413,6 +418,8 @@ int optifax_destroy(optifax_handle h) {
     if (h->d_desc) cudaFree(h->d_desc);
     if (h->d_grid_flags) cudaFree(h->d_grid_flags);
     if (h->d_xch) cudaFree(h->d_xch);
+    if (h->d_gnlse_desc) cudaFree(h->d_gnlse_desc);
+    if (h->d_gnlse_k) cudaFree(h->d_gnlse_k);
     for (auto s_ : h->side) cudaStreamDestroy(s_);
     for (auto e_ : h->ev) cudaEventDestroy(e_);
     delete h;
@@ -578,3 +585,63 @@ int optifax_opo_mex_batch(optifax_handle h,
 }
 
 }  // extern "C"
+
+// chi(3) fibre GNLSE (gnlsefib.m): validation, scratch, descriptors, launch
+extern "C" int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses, int32_t n_pulses,
+                             void* stream) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!pulses || n_pulses < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "gnlse: no pulses");
+    const int M = pulses[0].n_points, S = pulses[0].n_saves;
+    if (M != 512 && M != 1024 && M != 2048 && M != 4096)
+        return fail(h, OPTIFAX_ERR_UNSUPPORTED, "gnlse: n_points must be 512, 1024, 2048 or 4096");
+    std::vector<GnlseDev> d((size_t)n_pulses);
+    for (int i = 0; i < n_pulses; ++i) {
+        const optifax_gnlse_pulse& p = pulses[i];
+        if (p.n_points != M || p.n_saves != S)
+            return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "gnlse: pulses of one call share n_points and n_saves");
+        if (S < 2 || !p.A || !p.B || !p.W || !p.AT_out || !p.AW_out || !(p.length > 0.0) || !(p.dT > 0.0) ||
+            !(p.rtol > 0.0) || !(p.atol > 0.0) || !std::isfinite(p.gamma) || !std::isfinite(p.alpha) ||
+            !std::isfinite(p.fr) || (p.trace && p.trace_cap < 0))
+            return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "gnlse: pulse " + std::to_string(i) + " arguments");
+        GnlseDev& g = d[(size_t)i];
+        memset(&g, 0, sizeof(g));
+        g.A = (const float2*)p.A;
+        g.B = p.B;
+        g.W = p.W;
+        g.RW = (p.RW && p.fr != 0.0) ? (const float2*)p.RW : nullptr;
+        g.AT_out = (float2*)p.AT_out;
+        g.AW_out = (float2*)p.AW_out;
+        g.trace = (long long*)p.trace;
+        g.trace_cap = p.trace ? p.trace_cap : 0;
+        g.max_attempts = p.max_attempts > 0 ? p.max_attempts : 1000000;
+        g.stats = p.stats;
+        g.gamma = p.gamma; g.fr = p.fr; g.dT = p.dT; g.alpha = p.alpha; g.length = p.length;
+        g.rtol = p.rtol; g.atol = p.atol;
+        g.n_saves = S;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = OPTIFAX_OK;
+    const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
+    if (!twp) return rc;
+    const size_t need_k = (size_t)7 * M * n_pulses;
+    if (need_k > h->gnlse_k_cap) {
+        if (h->d_gnlse_k) { cudaDeviceSynchronize(); cudaFree(h->d_gnlse_k); h->d_gnlse_k = nullptr; h->gnlse_k_cap = 0; }
+        cudaError_t e = cudaMalloc(&h->d_gnlse_k, need_k * sizeof(float2));
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(gnlse stage scratch)");
+        h->gnlse_k_cap = need_k;
+    }
+    if ((size_t)n_pulses > h->gnlse_desc_cap) {
+        if (h->d_gnlse_desc) { cudaDeviceSynchronize(); cudaFree(h->d_gnlse_desc); h->d_gnlse_desc = nullptr; }
+        h->gnlse_desc_cap = 0;
+        cudaError_t e = cudaMalloc(&h->d_gnlse_desc, sizeof(GnlseDev) * (size_t)n_pulses);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(gnlse descriptors)");
+        h->gnlse_desc_cap = (size_t)n_pulses;
+    }
+    for (int i = 0; i < n_pulses; ++i) d[(size_t)i].K = h->d_gnlse_k + (size_t)7 * M * i;
+    cudaError_t e = cudaMemcpyAsync(h->d_gnlse_desc, d.data(), sizeof(GnlseDev) * (size_t)n_pulses,
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(gnlse descriptors)");
+    e = launch_gnlse(M, h->d_gnlse_desc, n_pulses, twp, twp + M, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "gnlse_kernel launch");
+    return OPTIFAX_OK;
+}

@@ -1,0 +1,346 @@
+// ofx_gnlse.cu -- chi(3) fibre GNLSE on the GPU: one persistent CTA per pulse.
+//
+// Replaces toolbox/lib/internal/main/gnlsefib.m:1-89.  The interaction-picture
+// spectral field AW (n modes, FFT order) obeys gnlsefib.m:54-66,
+//     dAW/dz = i gamma W ifft(AT ((1 - fR)|AT|^2 + RS)) e^{-Lz},
+//     AT = fft(AW e^{Lz}),  RS = dT fR fft(ifft(|AT|^2) RW),  L = iB - alpha/2,
+// in MATLAB's fft/ifft conventions (fft: exp(-i), ifft: exp(+i)/n), from
+// AW(0) = ifft(A).  The reference integrates it with MATLAB's ode45 (RelTol,
+// AbsTol, NormControl; gnlsefib.m:77-80); here an adaptive Dormand-Prince 5(4)
+// pair with the same tolerances and error norm,
+//     err = ||h sum_i e_i k_i|| / max(||y||, ||y_new||, AbsTol/RelTol) <= RelTol,
+// steps clamped to land on the save points (no interpolation), and positions
+// as integers in units of length / 2^40 so that every dispersion phase B_k z is
+// a 64-bit fixed-point product (exact mod one turn; only the final angle goes
+// through FP32).  FP32 field arithmetic, FP64 norms and step control.
+//
+// Layout: the CTA's M/16 threads hold the spectral state y in registers, 16
+// modes each, in the FFT's bit-reversed slot order (slot s <-> mode bitrev(s));
+// the time-domain fields live in two padded shared-memory buffers; the seven
+// stage derivatives k_i sit in an L2-resident global scratch (7 x n per pulse,
+// each thread touching only its own 128-byte rows).  Each right-hand side costs
+// four in-place M-point transforms (two without Raman): MATLAB's fft of a
+// spectral array is conj(inverse(conj(.))), its ifft (1/n) conj(forward(conj(.))).
+#include <cmath>
+#include <cstdint>
+
+#include "ofx_fft.cuh"
+#include "ofx_gnlse.cuh"
+
+namespace ofx {
+namespace {
+
+constexpr int kZBits = 40;
+
+// Dormand-Prince 5(4) tableau (Dormand & Prince 1980): nodes, stage weights
+// (row 6 = the 5th-order weights, FSAL), error weights b - b_hat.
+__constant__ double kDpC[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
+__constant__ float kDpA[7][6] = {
+    {0.f, 0.f, 0.f, 0.f, 0.f, 0.f},
+    {1.0f / 5, 0.f, 0.f, 0.f, 0.f, 0.f},
+    {3.0f / 40, 9.0f / 40, 0.f, 0.f, 0.f, 0.f},
+    {44.0f / 45, -56.0f / 15, 32.0f / 9, 0.f, 0.f, 0.f},
+    {19372.0f / 6561, -25360.0f / 2187, 64448.0f / 6561, -212.0f / 729, 0.f, 0.f},
+    {9017.0f / 3168, -355.0f / 33, 46732.0f / 5247, 49.0f / 176, -5103.0f / 18656, 0.f},
+    {35.0f / 384, 0.f, 500.0f / 1113, 125.0f / 192, -2187.0f / 6784, 11.0f / 84}};
+__constant__ float kDpE[7] = {71.0f / 57600, 0.f, -71.0f / 16695, 71.0f / 1920, -17253.0f / 339200,
+                              22.0f / 525, -1.0f / 40};
+
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// Sums of three per-thread values over the CTA in FP64; every thread gets them.
+template <int T>
+__device__ __forceinline__ void block_sum3(double a, double b, double c, double* red, double (&out)[3]) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    const int t = threadIdx.x;
+    __syncthreads();                       // red may still be read from the previous call
+    if ((t & 31) == 0) {
+        red[3 * (t >> 5)] = a;
+        red[3 * (t >> 5) + 1] = b;
+        red[3 * (t >> 5) + 2] = c;
+    }
+    __syncthreads();
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+#pragma unroll 1
+    for (int w = 0; w < T / 32; ++w) {     // fixed order: identical totals in every thread
+        s0 += red[3 * w];
+        s1 += red[3 * w + 1];
+        s2 += red[3 * w + 2];
+    }
+    out[0] = s0; out[1] = s1; out[2] = s2;
+}
+
+// Own 16 slots of stage array j in the global scratch (128 contiguous bytes)
+__device__ __forceinline__ const float4* krow(const float2* K, int M, int j, int t) {
+    return reinterpret_cast<const float4*>(K + (size_t)j * M + 16 * t);
+}
+
+}  // namespace
+
+template <int M>
+__global__ void __launch_bounds__(M / 16, 1)
+gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw1, const Twiddle* __restrict__ tw2) {
+    constexpr int T = M / 16;
+    constexpr int LOG2M = FftShape<M>::LOG2M;
+    constexpr int PADM = M + M / 16;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float2* bufA = reinterpret_cast<float2*>(smem);          // time domain: conj(AT), then conj(Q)
+    float2* bufB = bufA + PADM;                                // Raman: |AT|^2, then conj(RS / (dT fR))
+    uint64_t* rate_s = reinterpret_cast<uint64_t*>(bufB + PADM);   // B_k z per z unit, 2^-64 turns
+    float2* rw_s = reinterpret_cast<float2*>(rate_s + M);
+    float* w_s = reinterpret_cast<float*>(rw_s + M);
+    double* red = reinterpret_cast<double*>(w_s + M);
+
+    const int t = threadIdx.x;
+    __shared__ GnlseDev sP;
+    if (t == 0) sP = pulses[blockIdx.x];
+    __syncthreads();
+    const GnlseDev& P = sP;
+    const bool raman = (P.RW != nullptr);
+    const double unit = P.length / (double)(1ll << kZBits);
+    const long long total = 1ll << kZBits;
+    const long long hmax = total / 10;
+    const double thr = P.atol / P.rtol;
+    const float invM = 1.0f / (float)M;
+    const float gam = (float)P.gamma, omfr = (float)(1.0 - P.fr), dtfr = (float)(P.dT * P.fr);
+    const float awscale = (float)(P.dT * (double)M);
+    float2* K = P.K;
+
+    // per-mode tables in slot order (slot s holds mode bitrev(s))
+#pragma unroll 1
+    for (int j = 0; j < 16; ++j) {
+        const int slot = 16 * t + j;
+        const int k = bitrev(slot, LOG2M);
+        double r = P.B[k] * unit * 0.15915494309189533577;     // turns per z unit
+        r -= rint(r);
+        double x = r * 18446744073709551616.0;
+        if (x >= 9.2233720368547758e18) x -= 1.8446744073709552e19;
+        rate_s[slot] = (uint64_t)(long long)llrint(x);
+        w_s[slot] = P.W[k];
+        rw_s[slot] = raman ? P.RW[k] : make_float2(0.f, 0.f);
+    }
+    // y(0) = ifft(A) = conj(forward(conj(A))) / M
+#pragma unroll
+    for (int j = 0; j < 16; ++j) bufA[phys(16 * t + j)] = conjf2(P.A[16 * t + j]);
+    __syncthreads();
+    float2 y[16], ys[16], v[16], e[16];
+    fft_forward_to_regs<M>(bufA, tw1, tw2, t, v);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) y[j] = cscale(conjf2(v[j]), invM);
+
+    long long zc = 0, hc = 0, h = 0, target = 0;
+    int save_idx = 0, stage = 0, base = 0;
+    int attempts = 0, accepted = 0, status = 0;
+    bool save_now = true;
+    double ny = 0.0;
+    float hz = 0.f;
+
+    for (;;) {
+        if (save_now) {
+            // save `save_idx` at zc: AW e^{Lz} (fftshifted, x dT n) and AT = fft(AW e^{Lz})
+            const float att = expf((float)(-0.5 * P.alpha * (double)zc * unit));
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int slot = 16 * t + j;
+                const float2 aw = cscale(cmul(y[j], turn_to_unit(rate_s[slot] * (uint64_t)zc)), att);
+                const int k = bitrev(slot, LOG2M);
+                P.AW_out[(size_t)save_idx * M + ((k + M / 2) & (M - 1))] = cscale(aw, awscale);
+                v[j] = conjf2(aw);
+            }
+            fft_inverse_from_regs<M>(bufA, tw1, tw2, t, v);
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+                P.AT_out[(size_t)save_idx * M + 16 * t + j] = conjf2(bufA[phys(16 * t + j)]);
+            ++save_idx;
+            save_now = false;
+            if (save_idx == P.n_saves) break;
+        }
+        // ---- stage input ys and its position zs ----
+        long long zs = zc;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) ys[j] = y[j];
+        if (stage > 0) {
+            if (stage == 1) {
+                // next save point: i total / (n_saves - 1), rounded half up
+                target = ((long long)save_idx * total + (P.n_saves - 1) / 2) / (P.n_saves - 1);
+                hc = h < target - zc ? h : target - zc;
+                hz = (float)((double)hc * unit);
+            }
+#pragma unroll 1
+            for (int q = 0; q < stage; ++q) {
+                const float a = hz * kDpA[stage][q];
+                if (a == 0.f) continue;
+                const float4* kr = krow(K, M, (base + q) % 7, t);
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) {
+                    const float4 w = kr[jj];
+                    ys[2 * jj].x = fmaf(a, w.x, ys[2 * jj].x);
+                    ys[2 * jj].y = fmaf(a, w.y, ys[2 * jj].y);
+                    ys[2 * jj + 1].x = fmaf(a, w.z, ys[2 * jj + 1].x);
+                    ys[2 * jj + 1].y = fmaf(a, w.w, ys[2 * jj + 1].y);
+                }
+            }
+            zs = zc + llrint(kDpC[stage] * (double)hc);
+        }
+        // ---- right-hand side f(zs, ys) (gnlsefib.m:54-66) into v ----
+        {
+            const double zd = (double)zs * unit;
+            const float att = expf((float)(-0.5 * P.alpha * zd));
+            const float iatt = expf((float)(0.5 * P.alpha * zd));
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                e[j] = turn_to_unit(rate_s[16 * t + j] * (uint64_t)zs);      // e^{i B z}
+                v[j] = conjf2(cscale(cmul(ys[j], e[j]), att));
+            }
+            fft_inverse_from_regs<M>(bufA, tw1, tw2, t, v);                   // bufA = conj(AT)
+            if (raman) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const float2 c = bufA[phys(16 * t + j)];
+                    bufB[phys(16 * t + j)] = make_float2(c.x * c.x + c.y * c.y, 0.f);
+                }
+                __syncthreads();
+                fft_forward_to_regs<M>(bufB, tw1, tw2, t, v);                 // forward(|AT|^2)
+#pragma unroll
+                for (int j = 0; j < 16; ++j)                                  // conj(ifft(|AT|^2) RW)
+                    v[j] = conjf2(cscale(cmul(conjf2(v[j]), rw_s[16 * t + j]), invM));
+                fft_inverse_from_regs<M>(bufB, tw1, tw2, t, v);               // bufB = conj(RS / (dT fR))
+            }
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float2 at = conjf2(bufA[phys(16 * t + j)]);
+                const float it = at.x * at.x + at.y * at.y;
+                float2 g = make_float2(it, 0.f);
+                if (raman) {
+                    const float2 rb = bufB[phys(16 * t + j)];
+                    g = make_float2(fmaf(omfr, it, dtfr * rb.x), -dtfr * rb.y);
+                }
+                bufA[phys(16 * t + j)] = conjf2(cmul(at, g));                  // conj(Q)
+            }
+            __syncthreads();
+            fft_forward_to_regs<M>(bufA, tw1, tw2, t, v);                     // ifft(Q) = conj(v) / M
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float2 m = cmul(conjf2(v[j]), conjf2(e[j]));
+                const float s = gam * w_s[16 * t + j] * iatt * invM;
+                v[j] = make_float2(-m.y * s, m.x * s);                        // i gamma W M e^{-Lz}
+            }
+        }
+        {
+            float4* kw = reinterpret_cast<float4*>(K + (size_t)((base + stage) % 7) * M + 16 * t);
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj)
+                kw[jj] = make_float4(v[2 * jj].x, v[2 * jj].y, v[2 * jj + 1].x, v[2 * jj + 1].y);
+        }
+        if (stage == 0) {
+            // initial step: 0.8 rtol^(1/5) max(||y||, thr) / ||f||
+            double py = 0.0, pf = 0.0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                py += (double)(y[j].x * y[j].x + y[j].y * y[j].y);
+                pf += (double)(v[j].x * v[j].x + v[j].y * v[j].y);
+            }
+            double s3[3];
+            block_sum3<T>(py, pf, 0.0, red, s3);
+            ny = sqrt(s3[0]);
+            const double nf = sqrt(s3[1]);
+            if (nf == 0.0) h = hmax;
+            else {
+                double hh = (0.8 * pow(P.rtol, 0.2)) * fmax(ny, thr) / nf / unit;
+                long long hi = hh >= (double)hmax ? hmax : (long long)hh;
+                h = hi < 1 ? 1 : hi;
+            }
+            stage = 1;
+            continue;
+        }
+        if (stage < 6) { ++stage; continue; }
+
+        // ---- stage 6 done: ys = y_new, error estimate and decision ----
+        float2 ev[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) ev[j] = make_float2(0.f, 0.f);
+#pragma unroll 1
+        for (int q = 0; q < 7; ++q) {
+            const float a = hz * kDpE[q];
+            if (a == 0.f) continue;
+            const float4* kr = krow(K, M, (base + q) % 7, t);
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const float4 w = kr[jj];
+                ev[2 * jj].x = fmaf(a, w.x, ev[2 * jj].x);
+                ev[2 * jj].y = fmaf(a, w.y, ev[2 * jj].y);
+                ev[2 * jj + 1].x = fmaf(a, w.z, ev[2 * jj + 1].x);
+                ev[2 * jj + 1].y = fmaf(a, w.w, ev[2 * jj + 1].y);
+            }
+        }
+        double pe = 0.0, pn = 0.0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            pe += (double)(ev[j].x * ev[j].x + ev[j].y * ev[j].y);
+            pn += (double)(ys[j].x * ys[j].x + ys[j].y * ys[j].y);
+        }
+        double s3[3];
+        block_sum3<T>(pe, pn, 0.0, red, s3);
+        const double errn = sqrt(s3[0]), nyn = sqrt(s3[1]);
+        const double err = errn / fmax(fmax(ny, nyn), thr);
+        const bool ok = err <= P.rtol;
+        if (t == 0 && P.trace && attempts < P.trace_cap) {
+            P.trace[2 * attempts] = hc;
+            P.trace[2 * attempts + 1] = ok ? 1 : 0;
+        }
+        ++attempts;
+        if (!isfinite(errn) || !isfinite(nyn)) { status |= OPTIFAX_PULSE_NAN; break; }
+        const double fac = err == 0.0 ? 5.0 : 0.8 * pow(P.rtol / err, 0.2);
+        if (ok) {
+            ++accepted;
+            zc += hc;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) y[j] = ys[j];
+            ny = nyn;
+            base = (base + 6) % 7;                          // FSAL: k7 becomes the next k1
+            const double hh = (double)hc * fmin(5.0, fac);
+            const long long hi = hh >= (double)hmax ? hmax : (long long)hh;
+            h = hi < 1 ? 1 : hi;
+            if (zc == target) save_now = true;
+        } else {
+            const long long hi = (long long)((double)hc * fmax(0.1, fmin(1.0, fac)));
+            h = hi < 1 ? 1 : hi;
+        }
+        if (attempts >= P.max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; break; }
+        stage = 1;
+    }
+    if (t == 0 && P.stats) {
+        optifax_gnlse_stats st;
+        st.attempts = attempts; st.accepted = accepted; st.status = status; st.reserved = 0;
+        *P.stats = st;
+    }
+}
+
+template <int M>
+cudaError_t launch_one(const GnlseDev* d, int n_pulses, const Twiddle* tw1, const Twiddle* tw2, cudaStream_t st) {
+    constexpr int PADM = M + M / 16;
+    const size_t smem = sizeof(float2) * 2 * PADM + (sizeof(uint64_t) + sizeof(float2) + sizeof(float)) * M +
+                        sizeof(double) * 3 * (M / 16 / 32 > 0 ? M / 16 / 32 : 1);
+    cudaError_t e = cudaFuncSetAttribute(gnlse_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    gnlse_kernel<M><<<n_pulses, M / 16, smem, st>>>(d, tw1, tw2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gnlse(int M, const GnlseDev* d, int n_pulses, const Twiddle* tw1, const Twiddle* tw2,
+                         cudaStream_t st) {
+    switch (M) {
+        case 512: return launch_one<512>(d, n_pulses, tw1, tw2, st);
+        case 1024: return launch_one<1024>(d, n_pulses, tw1, tw2, st);
+        case 2048: return launch_one<2048>(d, n_pulses, tw1, tw2, st);
+        case 4096: return launch_one<4096>(d, n_pulses, tw1, tw2, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace ofx

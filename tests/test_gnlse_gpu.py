@@ -1,0 +1,103 @@
+"""chi(3) fibre GNLSE on the GPU (optifax_gnlse) against the FP64 oracle.  Marked gpu.
+
+The oracle replays the GPU's own (step, accepted) sequence, so the comparison is
+FP32 field arithmetic against FP64 on identical z positions; the GPU's own schedule
+is also compared with the oracle's.  Known answers on the GPU itself: a fundamental
+soliton keeps its shape and advances its phase by gamma P0 z / 2, and the photon
+number sum |AW|^2 / W is conserved with self-steepening and Raman scattering.
+"""
+import numpy as np
+import pytest
+
+from oracle import gnlse_oracle as go
+
+pytestmark = pytest.mark.gpu
+
+B2, GAMMA, T0, C0 = -1.183e-26, 0.11, 28.4e-15, 299792458.0
+BETAS = [B2, 8.1e-41, -9.5e-56]
+# measured on a GB300: 2.6e-7 .. 2.8e-7 over 1 cm (12 steps); FP32 rounding growing with the step count
+FIELD_TOL = 1e-5
+
+
+def _grid(n, window):
+    return np.arange(-n // 2, n // 2) * (window / n)
+
+
+def _run_gpu(T, A, w0, betas, loss, fr, RT, L, nsaves, trace_cap=100000):
+    from optifax_gb300 import gnlse
+    ops = gnlse.fibre_operators(T, w0, GAMMA, betas, loss, fr, RT)
+    r = gnlse.propagate(ops, A, L, nsaves, w0=w0, trace_cap=trace_cap)
+    st = r.stats[0]
+    tr = r.trace[0].cpu().numpy()[:st["attempts"]]
+    return r, st, [(int(h), int(a)) for h, a in tr]
+
+
+def test_gnlse_soliton_gpu():
+    n = 1024
+    T = _grid(n, 2e-12)
+    P0 = abs(B2) / (GAMMA * T0 ** 2)
+    A = np.sqrt(P0) / np.cosh(T / T0)
+    z0 = np.pi / 2 * T0 ** 2 / abs(B2)
+    r, st, _ = _run_gpu(T, A, 0.0, [B2], 0.0, 0.0, 0.0, 2 * z0, 5)
+    assert st["status"] == 0
+    AT = r.AT[0].cpu().numpy()
+    amp = max(np.max(np.abs(np.abs(AT[i]) - np.abs(A))) / np.sqrt(P0) for i in range(5))
+    ph = np.angle(AT[-1][n // 2] / A[n // 2])
+    expect = (GAMMA * P0 * r.Z[-1] / 2 + np.pi) % (2 * np.pi) - np.pi
+    print(dict(attempts=st["attempts"], amp_err=amp, phase_err=abs(ph - expect)))
+    assert amp < 1e-4
+    assert abs(ph - expect) < 1e-4
+
+
+@pytest.mark.parametrize("n,window,loss,L", [(1024, 2e-12, 0.0, 0.01), (2048, 4e-12, 0.5, 0.01),
+                                            (4096, 8e-12, 0.0, 0.01), (2048, 4e-12, 0.0, 0.08)])
+def test_gnlse_matches_oracle_on_gpu_schedule(n, window, loss, L):
+    T = _grid(n, window)
+    w0 = 2 * np.pi * C0 / 835e-9
+    A = np.sqrt(1000.0) / np.cosh(T / T0)
+    RT = go.raman_response(T)
+    nsaves = 5
+    r, st, steps = _run_gpu(T, A, w0, BETAS, loss, 0.18, RT, L, nsaves)
+    assert st["status"] == 0 and len(steps) == st["attempts"]
+    ops = go.gnlse_ops(T, w0, GAMMA, BETAS, loss, 0.18, RT)
+    A32 = np.asarray(A, np.complex64).astype(np.complex128)
+    ref = go.propagate(ops, A32, L, nsaves, forced=steps)
+    own = go.propagate(ops, A32, L, nsaves)
+    AT = r.AT[0].cpu().numpy().astype(np.complex128)
+    AW = r.AW[0].cpu().numpy().astype(np.complex128)
+    errs = [np.linalg.norm(AT[i] - ref.AT[i]) / np.linalg.norm(ref.AT[i]) for i in range(nsaves)]
+    aw_err = np.linalg.norm(AW[-1] - ref.AW[-1]) / np.linalg.norm(ref.AW[-1])
+    Wc = np.fft.fftshift(ops.W)
+    photons = [np.sum(np.abs(AW[i]) ** 2 / Wc) for i in range(nsaves)]
+    info = dict(n=n, attempts=st["attempts"], accepted=st["accepted"], oracle_own_attempts=own.attempts,
+                same_schedule=(own.steps == steps), field_err=max(errs), aw_err=aw_err,
+                photon_drift=photons[-1] / photons[0] - 1)
+    print(info)
+    assert max(errs) <= FIELD_TOL, info
+    assert aw_err <= FIELD_TOL, info
+    # photons: conserved by self-steepening and Raman scattering, lost only to the fibre loss
+    expect = 10.0 ** (-loss * L / 10.0)
+    assert abs(photons[-1] / photons[0] / expect - 1) < 1e-6, info
+
+
+def test_gnlse_batch_matches_single_runs():
+    from optifax_gb300 import gnlse
+    n = 1024
+    T = _grid(n, 2e-12)
+    w0 = 2 * np.pi * C0 / 835e-9
+    RT = go.raman_response(T)
+    ops = gnlse.fibre_operators(T, w0, GAMMA, BETAS, 0.0, 0.18, RT)
+    A = np.stack([np.sqrt(p) / np.cosh(T / T0) for p in (400.0, 900.0)])
+    both = gnlse.propagate(ops, A, 0.01, 3, w0=w0)
+    for b in range(2):
+        one = gnlse.propagate(ops, A[b], 0.01, 3, w0=w0)
+        assert both.stats[b] == one.stats[0]
+        assert np.array_equal(both.AT[b].cpu().numpy(), one.AT[0].cpu().numpy())
+
+
+def test_gnlse_rejects_unsupported_size():
+    from optifax_gb300 import gnlse, _native as nat
+    T = _grid(1000, 2e-12)
+    ops = gnlse.fibre_operators(T, 0.0, GAMMA, [B2], 0.0, 0.0, 0.0)
+    with pytest.raises(nat.OptifaxError):
+        gnlse.propagate(ops, np.ones(1000), 0.01, 3)

@@ -1,0 +1,70 @@
+"""The GNLSE oracle (oracle/gnlse_oracle.py) against known answers, on the CPU.
+
+gnlsefib.m's own integrator is MATLAB's ode45 (not available), so parity is
+unpinned; these checks establish that the restated equation and conventions are
+right: a fundamental soliton keeps its shape and advances its phase by
+gamma P0 z / 2 (anomalous dispersion, no Raman, no shock), pure dispersion with
+loss is exact, the photon number sum |AW|^2 / W is conserved with self-steepening
+and Raman scattering, and a recorded schedule replays bit for bit.
+"""
+import numpy as np
+import pytest
+
+from oracle import gnlse_oracle as go
+
+B2, GAMMA, T0 = -1.183e-26, 0.11, 28.4e-15
+
+
+def _grid(n=1024, window=2e-12):
+    return np.arange(-n // 2, n // 2) * (window / n)
+
+
+def test_fundamental_soliton():
+    T = _grid()
+    P0 = abs(B2) / (GAMMA * T0 ** 2)
+    A = np.sqrt(P0) / np.cosh(T / T0)
+    ops = go.gnlse_ops(T, 0.0, GAMMA, [B2], 0.0, 0.0, 0.0)
+    z0 = np.pi / 2 * T0 ** 2 / abs(B2)                 # soliton period
+    r = go.propagate(ops, A, 2 * z0, 5)
+    for i, z in enumerate(r.Z):
+        assert np.max(np.abs(np.abs(r.AT[i]) - np.abs(A))) / np.sqrt(P0) < 2e-5
+        ph = np.angle(r.AT[i][len(T) // 2] / A[len(T) // 2])
+        expect = (GAMMA * P0 * z / 2 + np.pi) % (2 * np.pi) - np.pi
+        assert abs(ph - expect) < 1e-5
+
+
+def test_dispersion_and_loss_exact():
+    T = _grid()
+    A = 30.0 / np.cosh(T / T0) * np.exp(1j * 0.3 * T / T0)
+    ops = go.gnlse_ops(T, 0.0, 0.0, [B2, 8e-41], 1.5, 0.0, 0.0)
+    z = 0.05
+    r = go.propagate(ops, A, z, 3)
+    exact = np.fft.fft(np.fft.ifft(A) * np.exp(-0.5 * ops.alpha * z) * np.exp(1j * ops.B * z))
+    assert np.linalg.norm(r.AT[-1] - exact) / np.linalg.norm(exact) < 1e-13
+
+
+def test_photon_number_conserved_with_shock_and_raman():
+    n = 2048
+    T = _grid(n, 4e-12)
+    w0 = 2 * np.pi * 299792458.0 / 835e-9
+    P0 = 600.0
+    A = np.sqrt(P0) / np.cosh(T / T0)
+    RT = go.raman_response(T)
+    ops = go.gnlse_ops(T, w0, GAMMA, [B2, 8.1e-41, -9.5e-56], 0.0, 0.18, RT)
+    r = go.propagate(ops, A, 0.01, 3)
+    Wabs = np.fft.fftshift(ops.W)                      # centred V + w0
+    photons = [np.sum(np.abs(aw) ** 2 / Wabs) for aw in r.AW]
+    assert abs(photons[-1] / photons[0] - 1) < 1e-8
+    energy = [np.sum(np.abs(aw) ** 2) for aw in r.AW]
+    assert abs(energy[-1] / energy[0] - 1) > 1e-5      # Raman moves energy (to the red): not conserved
+
+
+def test_replay_reproduces_schedule():
+    T = _grid(512, 1.5e-12)
+    A = np.sqrt(300.0) / np.cosh(T / T0)
+    ops = go.gnlse_ops(T, 0.0, GAMMA, [B2], 0.0, 0.0, 0.0)
+    a = go.propagate(ops, A, 0.05, 4)
+    b = go.propagate(ops, A, 0.05, 4, forced=a.steps)
+    assert a.steps == b.steps
+    assert np.array_equal(a.AT, b.AT)
+    assert any(ok == 0 for _, ok in a.steps) or a.attempts == a.accepted

@@ -51,3 +51,31 @@ def test_create_without_gpu_fails_cleanly():
     lib = nat.load()
     h = ctypes.c_void_p()
     assert lib.optifax_create(ctypes.byref(h), 0) == 3
+
+
+def test_struct_layouts_match_ctypes(tmp_path):
+    """The ctypes mirrors of the ABI structs have the C compiler's offsets and sizes."""
+    import shutil
+    import subprocess
+    from optifax_gb300 import _native as nat
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"optifax_gnlse_pulse": nat.OptifaxGnlsePulse, "optifax_gnlse_stats": nat.OptifaxGnlseStats,
+               "optifax_pulse": nat.OptifaxPulse, "optifax_setup": nat.OptifaxSetup}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "optifax.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
