@@ -32,19 +32,9 @@ namespace {
 
 constexpr int kZBits = 40;
 
-// Dormand-Prince 5(4) tableau (Dormand & Prince 1980): nodes, stage weights
-// (row 6 = the 5th-order weights, FSAL), error weights b - b_hat.
+// Dormand-Prince 5(4) tableau (Dormand & Prince 1980): nodes here; stage weights
+// (row 6 = the 5th-order weights, FSAL) and error weights b - b_hat below (kA, kE).
 __constant__ double kDpC[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.0};
-__constant__ float kDpA[7][6] = {
-    {0.f, 0.f, 0.f, 0.f, 0.f, 0.f},
-    {1.0f / 5, 0.f, 0.f, 0.f, 0.f, 0.f},
-    {3.0f / 40, 9.0f / 40, 0.f, 0.f, 0.f, 0.f},
-    {44.0f / 45, -56.0f / 15, 32.0f / 9, 0.f, 0.f, 0.f},
-    {19372.0f / 6561, -25360.0f / 2187, 64448.0f / 6561, -212.0f / 729, 0.f, 0.f},
-    {9017.0f / 3168, -355.0f / 33, 46732.0f / 5247, 49.0f / 176, -5103.0f / 18656, 0.f},
-    {35.0f / 384, 0.f, 500.0f / 1113, 125.0f / 192, -2187.0f / 6784, 11.0f / 84}};
-__constant__ float kDpE[7] = {71.0f / 57600, 0.f, -71.0f / 16695, 71.0f / 1920, -17253.0f / 339200,
-                              22.0f / 525, -1.0f / 40};
 
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
@@ -78,6 +68,66 @@ __device__ __forceinline__ void block_sum3(double a, double b, double c, double*
 // Own 16 slots of stage array j in the global scratch (128 contiguous bytes)
 __device__ __forceinline__ const float4* krow(const float2* K, int M, int j, int t) {
     return reinterpret_cast<const float4*>(K + (size_t)j * M + 16 * t);
+}
+
+// The same tableau as compile-time values, so that the stage combinations unroll
+// (all their L2 loads in flight together) and skip the zero weights.
+__host__ __device__ constexpr float dp_a(int r, int q) {
+    switch (r * 8 + q) {
+        case 8: return 1.0f / 5;
+        case 16: return 3.0f / 40;
+        case 17: return 9.0f / 40;
+        case 24: return 44.0f / 45;
+        case 25: return -56.0f / 15;
+        case 26: return 32.0f / 9;
+        case 32: return 19372.0f / 6561;
+        case 33: return -25360.0f / 2187;
+        case 34: return 64448.0f / 6561;
+        case 35: return -212.0f / 729;
+        case 40: return 9017.0f / 3168;
+        case 41: return -355.0f / 33;
+        case 42: return 46732.0f / 5247;
+        case 43: return 49.0f / 176;
+        case 44: return -5103.0f / 18656;
+        case 48: return 35.0f / 384;
+        case 50: return 500.0f / 1113;
+        case 51: return 125.0f / 192;
+        case 52: return -2187.0f / 6784;
+        case 53: return 11.0f / 84;
+        default: return 0.f;
+    }
+}
+__host__ __device__ constexpr float dp_e(int q) {
+    switch (q) {
+        case 0: return 71.0f / 57600;
+        case 2: return -71.0f / 16695;
+        case 3: return 71.0f / 1920;
+        case 4: return -17253.0f / 339200;
+        case 5: return 22.0f / 525;
+        case 6: return -1.0f / 40;
+        default: return 0.f;
+    }
+}
+
+// acc += sum_q w_q h K[(base + q) % 7] over the compile-time weights w_q (row R of
+// kA, or kE when R < 0), q < NQ
+template <int R, int NQ>
+__device__ __forceinline__ void combine(float2 (&acc)[16], const float2* K, int M, int t, int base, float hz) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const float wq = (R >= 0) ? dp_a(R, q) : dp_e(q);
+        if (wq == 0.f) continue;
+        const float a = hz * wq;
+        const float4* kr = krow(K, M, (base + q) % 7, t);
+#pragma unroll
+        for (int jj = 0; jj < 8; ++jj) {
+            const float4 w = kr[jj];
+            acc[2 * jj].x = fmaf(a, w.x, acc[2 * jj].x);
+            acc[2 * jj].y = fmaf(a, w.y, acc[2 * jj].y);
+            acc[2 * jj + 1].x = fmaf(a, w.z, acc[2 * jj + 1].x);
+            acc[2 * jj + 1].y = fmaf(a, w.w, acc[2 * jj + 1].y);
+        }
+    }
 }
 
 }  // namespace
@@ -171,19 +221,13 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
                 hc = h < target - zc ? h : target - zc;
                 hz = (float)((double)hc * unit);
             }
-#pragma unroll 1
-            for (int q = 0; q < stage; ++q) {
-                const float a = hz * kDpA[stage][q];
-                if (a == 0.f) continue;
-                const float4* kr = krow(K, M, (base + q) % 7, t);
-#pragma unroll
-                for (int jj = 0; jj < 8; ++jj) {
-                    const float4 w = kr[jj];
-                    ys[2 * jj].x = fmaf(a, w.x, ys[2 * jj].x);
-                    ys[2 * jj].y = fmaf(a, w.y, ys[2 * jj].y);
-                    ys[2 * jj + 1].x = fmaf(a, w.z, ys[2 * jj + 1].x);
-                    ys[2 * jj + 1].y = fmaf(a, w.w, ys[2 * jj + 1].y);
-                }
+            switch (stage) {
+                case 1: combine<1, 1>(ys, K, M, t, base, hz); break;
+                case 2: combine<2, 2>(ys, K, M, t, base, hz); break;
+                case 3: combine<3, 3>(ys, K, M, t, base, hz); break;
+                case 4: combine<4, 4>(ys, K, M, t, base, hz); break;
+                case 5: combine<5, 5>(ys, K, M, t, base, hz); break;
+                default: combine<6, 6>(ys, K, M, t, base, hz); break;
             }
             zs = zc + llrint(kDpC[stage] * (double)hc);
         }
@@ -264,20 +308,7 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
         float2 ev[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) ev[j] = make_float2(0.f, 0.f);
-#pragma unroll 1
-        for (int q = 0; q < 7; ++q) {
-            const float a = hz * kDpE[q];
-            if (a == 0.f) continue;
-            const float4* kr = krow(K, M, (base + q) % 7, t);
-#pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-                const float4 w = kr[jj];
-                ev[2 * jj].x = fmaf(a, w.x, ev[2 * jj].x);
-                ev[2 * jj].y = fmaf(a, w.y, ev[2 * jj].y);
-                ev[2 * jj + 1].x = fmaf(a, w.z, ev[2 * jj + 1].x);
-                ev[2 * jj + 1].y = fmaf(a, w.w, ev[2 * jj + 1].y);
-            }
-        }
+        combine<-1, 7>(ev, K, M, t, base, hz);
         double pe = 0.0, pn = 0.0;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
