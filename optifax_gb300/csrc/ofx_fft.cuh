@@ -239,39 +239,4 @@ __device__ __forceinline__ void fft_inverse_from_regs(float2* buf, const Twiddle
     __syncthreads();
 }
 
-// dif_stages/dit_stages over a twiddle table W_MT^e (used by the cluster
-// exchange, whose C-point DFT runs on the N-point table).
-template <int MT, int R, int L>
-__device__ __forceinline__ void dif_stages(float2* v, int off, const Twiddle* __restrict__ tw) {
-#pragma unroll
-    for (int hr = R / 2; hr >= 1; hr >>= 1) {
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            if (q & hr) continue;
-            int o = off + (q & (hr - 1)) * (L / R);
-            int e = o * (R / (2 * hr)) * (MT / L);
-            float2 a = v[q], b = v[q + hr];
-            v[q] = cadd(a, b);
-            v[q + hr] = tw_fwd(csub(a, b), tw[e]);
-        }
-    }
-}
-
-template <int MT, int R, int L>
-__device__ __forceinline__ void dit_stages(float2* v, int off, const Twiddle* __restrict__ tw) {
-#pragma unroll
-    for (int hr = 1; hr <= R / 2; hr <<= 1) {
-#pragma unroll
-        for (int q = 0; q < R; ++q) {
-            if (q & hr) continue;
-            int o = off + (q & (hr - 1)) * (L / R);
-            int e = o * (R / (2 * hr)) * (MT / L);
-            float2 a = v[q];
-            float2 t = tw_inv(v[q + hr], tw[e]);
-            v[q] = cadd(a, t);
-            v[q + hr] = csub(a, t);
-        }
-    }
-}
-
 }  // namespace ofx
