@@ -118,3 +118,37 @@ def test_nee_semantics_run(oracle):
     mex = _run(oracle, si, E[0])
     # same physics, different conventions: close but not identical
     assert 0 < rel_l2(r.A[0], mex.A[0]) < 0.5
+
+
+def _shg_case(a1):
+    """Undepleted second-harmonic generation on an exact grid: w0 on bin 100, a weak
+    tone on bin 20, so the A^2 e^{i w0 t} drive puts the harmonic on bin 140; one
+    domain (constant G), and the only dispersion a phase delta per step on bin 140,
+    so the phase mismatch is delta per step."""
+    N, dt, h = 1024, 1e-15, 1e-7
+    n = np.arange(N)
+    beta = np.zeros(N)
+    beta[140] = 4 * np.pi / 2000
+    return dict(N=N, dt=dt, h=h, w0=2 * np.pi * 100 / (N * dt), E=a1 * np.exp(2j * np.pi * 20 * n / N),
+                alpha=np.ones(N), beta=beta, delta=beta[140])
+
+
+def test_undepleted_shg_follows_sinc(oracle):
+    """Known answer (the idea of sincgain.m, derived independently): with a constant
+    source and mismatch dk, the harmonic grows as |sin(dk z/2) / (dk/2)| through two
+    full lobes, z being the propagated length (the sum of the accepted step sizes:
+    the reference's chunk-end rule ends a pass a few steps past n_steps).  minErr = 0
+    keeps the steps uniform."""
+    c = _shg_case(1e-3)
+    out = []
+    for S in [100, 300, 500, 700, 900, 996, 1100, 1300, 1500, 1800, 1996]:
+        r = oracle.run(c["E"], c["alpha"], np.full(S, 1e3), c["beta"], w0=c["w0"], bdiffw0=0.0, h=c["h"],
+                       n_steps=S, dt=c["dt"], max_err=1e-6, min_err=0.0, sel=float(S),
+                       time_mode=oracle.TIME_UNSHIFTED, abc_mode=oracle.ABC_NONE, chunk_mode=oracle.CHUNKS_TRUNC)
+        z = r.stats[0]["z_steps"]
+        sh = abs(np.fft.fft(r.A[0])[140]) / c["N"]
+        out.append((sh, abs(np.sin(c["delta"] * z / 2) / (c["delta"] / 2))))
+    k = out[0][0] / out[0][1]
+    peak = k * 2 / c["delta"]
+    dev = max(abs(sh - k * p) for sh, p in out) / peak
+    assert dev < 1e-5, dev
