@@ -329,9 +329,11 @@ constexpr bool kPullGather = (C <= 4);
 // of up to 4) or from global memory (`xx`, all loads in flight) -- computes the
 // C-point DFTs and stores the results in their owners' shared memory (`buf`, the
 // owner's FFT buffer, at phys(n2)) or, for 16-CTA clusters, in their blocks of
-// `yy` (global).  Ordering comes
-// from the cluster barriers around the calls (release/acquire at cluster scope
-// covers global and distributed shared memory); global accesses bypass L1.
+// `yy` (global).  Ordering comes from the cluster barriers around the calls
+// (release/acquire at cluster scope covers global and distributed shared memory):
+// the stage outputs are complete at the error-flag barrier before the call, and no
+// CTA reads its FFT buffer again until the barrier after it.  Global accesses
+// bypass L1.
 template <int M, int C>
 __device__ __forceinline__ void exchange_forward_g(const float2* __restrict__ xx, const float2* bufe,
                                                    float2* buf, float2* yy,
