@@ -90,6 +90,10 @@ def propagate(ops: FibreOperators, A, flength: float, nsaves: int, *, w0: float 
     dev = torch.device(f"cuda:{device}")
     A = torch.as_tensor(np.ascontiguousarray(np.atleast_2d(A), dtype=np.complex64)).to(dev) \
         if not isinstance(A, torch.Tensor) else torch.atleast_2d(A).to(dev, torch.complex64).contiguous()
+    if A.dim() != 2 or A.shape[1] != n:
+        raise nat.OptifaxError(f"gnlse: input fields must have {n} points (the operators' grid)")
+    if nsaves < 2:
+        raise nat.OptifaxError("gnlse: nsaves must be at least 2 (z = 0 and z = flength)")
     nb = A.shape[0]
     B_d = torch.from_numpy(np.ascontiguousarray(ops.B)).to(dev)
     W_d = torch.from_numpy(np.ascontiguousarray(ops.W, dtype=np.float32)).to(dev)

@@ -50,8 +50,9 @@ def test_gnlse_soliton_gpu():
     assert abs(ph - expect) < 1e-4
 
 
-@pytest.mark.parametrize("n,window,loss,L", [(1024, 2e-12, 0.0, 0.01), (2048, 4e-12, 0.5, 0.01),
-                                            (4096, 8e-12, 0.0, 0.01), (2048, 4e-12, 0.0, 0.08)])
+@pytest.mark.parametrize("n,window,loss,L", [(512, 1.5e-12, 0.0, 0.01), (1024, 2e-12, 0.0, 0.01),
+                                            (2048, 4e-12, 0.5, 0.01), (4096, 8e-12, 0.0, 0.01),
+                                            (2048, 4e-12, 0.0, 0.08)])
 def test_gnlse_matches_oracle_on_gpu_schedule(n, window, loss, L):
     T = _grid(n, window)
     w0 = 2 * np.pi * C0 / 835e-9
@@ -105,3 +106,8 @@ def test_gnlse_rejects_unsupported_size():
     ops = gnlse.fibre_operators(T, 0.0, GAMMA, [B2], 0.0, 0.0, 0.0)
     with pytest.raises(nat.OptifaxError):
         gnlse.propagate(ops, np.ones(1000), 0.01, 3)
+    ops = gnlse.fibre_operators(_grid(1024, 2e-12), 0.0, GAMMA, [B2], 0.0, 0.0, 0.0)
+    with pytest.raises(nat.OptifaxError):
+        gnlse.propagate(ops, np.ones(512), 0.01, 3)          # field shorter than the grid
+    with pytest.raises(nat.OptifaxError):
+        gnlse.propagate(ops, np.ones(1024), 0.01, 1)         # a single save
