@@ -12,7 +12,6 @@ Dormand-Prince 5(4) pair with the tolerances the reference gives ode45 (RelTol
 """
 from __future__ import annotations
 
-import ctypes
 import math
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
