@@ -41,6 +41,7 @@ def test_status_strings_and_null_handle():
     assert lib.optifax_status_string(1) == b"invalid argument"
     assert lib.optifax_destroy(None) == 5
     assert lib.optifax_propagate(None, None, 0, 0, 0, 0, None, None) == 5
+    assert lib.optifax_gnlse(None, None, 0, None) == 5
 
 
 def test_create_without_gpu_fails_cleanly():
