@@ -284,6 +284,9 @@ int optifax_fno_forward(optifax_fno f, const float* x, float* y, int32_t batch, 
  * (DEVICE, param_count floats) are optional copies of the results */
 int optifax_fno_backward(optifax_fno f, const float* x, const float* target, const float* sample_w,
                          int32_t batch, float* loss, float* grads, void* stream);
+/* replace the gradients of the last backward (DEVICE, param_count floats), e.g. by their
+ * mean over data-parallel ranks, before optifax_fno_adam */
+int optifax_fno_set_grads(optifax_fno f, const float* grads, void* stream);
 /* AdamW step (decoupled weight decay) with the gradients of the last backward; step >= 1 */
 int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta2, float eps,
                      float weight_decay, int32_t step, void* stream);

@@ -21,7 +21,7 @@ EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifa
            "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
            "optifax_ff_encode", "optifax_ff_step",
            "optifax_ff_encode_env", "optifax_ff_decode_env", "optifax_setup_work_bytes", "optifax_setup_pulses",
-           "optifax_gnlse"]
+           "optifax_gnlse", "optifax_fno_set_grads"]
 
 _lib = None
 
@@ -103,6 +103,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_fno_forward.restype = ctypes.c_int
     lib.optifax_fno_backward.argtypes = [vp, vp, vp, vp, i32, vp, vp, vp]
     lib.optifax_fno_backward.restype = ctypes.c_int
+    lib.optifax_fno_set_grads.argtypes = [vp, vp, vp]
+    lib.optifax_fno_set_grads.restype = ctypes.c_int
     lib.optifax_fno_adam.argtypes = [vp, f32, f32, f32, f32, f32, i32, vp]
     lib.optifax_fno_adam.restype = ctypes.c_int
     lib.optifax_ff_encode.argtypes = [vp, i64, i32, i32, i32, i32, i32, f32, vp, vp, i32, vp, vp]

@@ -838,6 +838,15 @@ extern "C" int optifax_fno_backward(optifax_fno f, const float* x, const float* 
     return OPTIFAX_OK;
 }
 
+// Data-parallel training: replace the gradients of the last backward (for example by
+// their mean over ranks) before optifax_fno_adam.
+extern "C" int optifax_fno_set_grads(optifax_fno f, const float* grads, void* stream) {
+    if (!f) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!grads) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    return cudaMemcpyAsync(f->grad, grads, sizeof(float) * N_PARAMS, cudaMemcpyDeviceToDevice,
+                           static_cast<cudaStream_t>(stream)) == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
 extern "C" int optifax_fno_adam(optifax_fno f, float lr, float beta1, float beta2, float eps, float weight_decay,
                                 int32_t step, void* stream) {
     if (!f) return OPTIFAX_ERR_NULL_HANDLE;

@@ -6,8 +6,10 @@ pairs) are independent units: each rank takes a contiguous range of instances,
 balanced by the cost N log2(N) S (grid points x transform depth x steps), runs it
 with no collective on the data path, and rank 0 gathers the results once at the
 end.  A single OPO cavity is sequential in round trips, so cavities only run as
-independent replicas (one per rank).  No reference counterpart: OptiFax runs on
-one MATLAB process (its NumOfParRuns pulses share one batched MEX call).
+independent replicas (one per rank).  Surrogate training is data parallel: each
+rank takes its shard of the training pairs and the gradients are averaged over
+the ranks every step (all_reduce_mean_).  No reference counterpart: OptiFax runs
+on one MATLAB process (its NumOfParRuns pulses share one batched MEX call).
 """
 from __future__ import annotations
 
@@ -70,6 +72,16 @@ def max_over_ranks(value: float, device: Optional[torch.device] = None) -> float
     t = torch.tensor([float(value)], dtype=torch.float64, device=device or torch.device("cpu"))
     torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     return float(t.item())
+
+
+def all_reduce_mean_(t: torch.Tensor) -> torch.Tensor:
+    """In place: the mean of `t` over all ranks (a no-op on one rank)."""
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        world = torch.distributed.get_world_size()
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+            t.div_(world)
+    return t
 
 
 def gather_to_rank0(obj) -> Optional[list]:

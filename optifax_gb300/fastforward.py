@@ -279,7 +279,18 @@ def evaluate(net: FNO, X: torch.Tensor, T: torch.Tensor, batch: Optional[int] = 
 def train(net: FNO, X: torch.Tensor, T: torch.Tensor, *, epochs: int = 40, batch: int = 32, lr: float = 1e-3,
           val_frac: float = 0.05, seed: int = 3, weight_decay: float = 0.0, trip_idx=None, log=None) -> dict:
     """AdamW with cosine-decayed learning rate on shuffled minibatches, relative
-    (per-sample weighted) squared error; returns the history."""
+    (per-sample weighted) squared error; returns the history.  Data parallel over the
+    ranks of an initialised process group: every rank draws the same minibatch order
+    (one seed), trains on its slice of each global minibatch (batch / world samples)
+    and applies the gradients averaged over the ranks (surrogate.data_parallel_step),
+    so the replicas stay identical; X and T are the full pair set on every rank."""
+    from .surrogate import data_parallel_step
+    world = (torch.distributed.get_world_size()
+             if torch.distributed.is_available() and torch.distributed.is_initialized() else 1)
+    rank = torch.distributed.get_rank() if world > 1 else 0
+    if batch % world:
+        raise ValueError("the global batch must be a multiple of the number of ranks")
+    local = batch // world
     P = X.shape[0]
     g = torch.Generator().manual_seed(seed)
     perm = torch.randperm(P, generator=g)
@@ -296,11 +307,10 @@ def train(net: FNO, X: torch.Tensor, T: torch.Tensor, *, epochs: int = 40, batch
         order = tr[torch.randperm(len(tr), generator=g)]
         acc = torch.zeros(1, device=net.dev)
         for s_ in range(steps_per_epoch):
-            idx = order[s_ * batch:(s_ + 1) * batch].to(net.dev)
-            loss = net.backward(X.index_select(0, idx), T.index_select(0, idx), sample_w=Wt.index_select(0, idx))
-            acc += loss
+            idx = order[s_ * batch:(s_ + 1) * batch][rank * local:(rank + 1) * local].to(net.dev)
             cur = lr * 0.5 * (1.0 + math.cos(math.pi * step_i / total))
-            net.adam(cur, weight_decay=weight_decay)
+            acc += data_parallel_step(net, X.index_select(0, idx), T.index_select(0, idx), cur,
+                                      sample_w=Wt.index_select(0, idx), weight_decay=weight_decay)
             step_i += 1
         hist["train_loss"].append(float(acc.item()) / steps_per_epoch)
         ve = evaluate(net, X[vdev], T[vdev])

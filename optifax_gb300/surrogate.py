@@ -114,6 +114,13 @@ class FNO:
                   None, "fno_backward")
         return self.loss_dev
 
+    def set_grads(self, grads: torch.Tensor, stream=None):
+        """Replace the gradients of the last backward (e.g. by their mean over ranks)."""
+        if grads.dtype != torch.float32 or grads.numel() != N_PARAMS or grads.device != self.dev:
+            raise ValueError("grads must be float32, one per parameter, on the network's device")
+        nat.check(self.lib.optifax_fno_set_grads(self.h, grads.contiguous().data_ptr(), self._s(stream)), None,
+                  "fno_set_grads")
+
     def adam(self, lr: float, betas=(0.9, 0.999), eps: float = 1e-8, weight_decay: float = 0.0, stream=None):
         self.step += 1
         nat.check(self.lib.optifax_fno_adam(self.h, float(lr), float(betas[0]), float(betas[1]), float(eps),
@@ -129,3 +136,26 @@ class FNO:
             self.close()
         except Exception:
             pass
+
+
+def data_parallel_step(net, x, target, lr: float, *, sample_w=None, weight_decay: float = 0.0, grads=None,
+                       reduce=None):
+    """One data-parallel training step: forward + backward on this rank's shard, the
+    gradients averaged over the ranks (``reduce``, default dist.all_reduce_mean_),
+    then AdamW on every rank with the same gradients, so the replicas stay
+    identical.  With one rank this is the plain step.  Each rank's loss is normalised
+    by its own shard, so equal shard sizes give exactly the full-batch gradient."""
+    from . import dist
+    reduce = reduce or dist.all_reduce_mean_
+    world = (torch.distributed.get_world_size()
+             if torch.distributed.is_available() and torch.distributed.is_initialized() else 1)
+    if world == 1 and reduce is dist.all_reduce_mean_:
+        loss = net.backward(x, target, sample_w=sample_w)
+    else:
+        if grads is None:
+            grads = torch.empty(N_PARAMS, dtype=torch.float32, device=x.device)
+        loss = net.backward(x, target, grads=grads, sample_w=sample_w)
+        reduce(grads)
+        net.set_grads(grads)
+    net.adam(lr, weight_decay=weight_decay)
+    return loss

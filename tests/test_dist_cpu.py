@@ -55,3 +55,74 @@ def test_two_rank_shard_gather_and_max_time():
     assert [g["rank"] for g in got] == [0, 1]
     assert got[0]["items"] + got[1]["items"] == list(range(20))
     assert abs(got[0]["work"] - got[1]["work"]) <= 20
+
+
+class _OracleNet:
+    """Stand-in for the GPU network with the FP64 oracle's gradients (CPU), for the
+    data-parallel step's host logic: backward, set_grads and a plain gradient step."""
+
+    def __init__(self, params):
+        import numpy as np
+        self.p = np.array(params, dtype=np.float64)
+        self.grad = None
+        self.dev = torch.device("cpu")
+
+    def backward(self, x, target, grads=None, sample_w=None):
+        from oracle import fno_oracle
+        loss, g, _ = fno_oracle.loss_and_grads(self.p, x.numpy(), target.numpy(), weights_bf16=False,
+                                               sample_w=None if sample_w is None else sample_w.numpy())
+        self.grad = g
+        if grads is not None:
+            grads.copy_(torch.from_numpy(g.astype("float32")))
+        return torch.tensor([loss], dtype=torch.float32)
+
+    def set_grads(self, grads):
+        self.grad = grads.numpy().astype("float64")
+
+    def adam(self, lr, weight_decay=0.0):
+        self.p -= lr * self.grad
+
+
+def _dp_case():
+    import numpy as np
+    from optifax_gb300 import surrogate
+    g = np.random.default_rng(5)
+    x = torch.from_numpy(g.standard_normal((4, surrogate.CIN, 64)).astype("float32"))
+    t = torch.from_numpy(g.standard_normal((4, surrogate.COUT, 64)).astype("float32"))
+    w = torch.from_numpy(g.uniform(0.5, 2.0, 4).astype("float32"))
+    return surrogate.init_params(1), x, t, w
+
+
+def _dp_worker(rank, world, port, out_dir):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    from optifax_gb300 import dist, surrogate
+    r, w_, _ = dist.init("gloo")
+    params, x, t, w = _dp_case()
+    net = _OracleNet(params)
+    sl = slice(2 * r, 2 * r + 2)                    # this rank's half of the global batch of 4
+    grads = torch.empty(surrogate.N_PARAMS, dtype=torch.float32)
+    surrogate.data_parallel_step(net, x[sl], t[sl], 1e-3, sample_w=w[sl], grads=grads)
+    got = dist.gather_to_rank0({"rank": r, "p": net.p, "g": grads.numpy().copy()})
+    dist.barrier()
+    if r == 0:
+        import pickle
+        with open(os.path.join(out_dir, "dp.pkl"), "wb") as f:
+            pickle.dump(got, f)
+    torch.distributed.destroy_process_group()
+
+
+def test_two_rank_data_parallel_surrogate_step():
+    """Gradients averaged over 2 ranks (halves of the batch) equal the full-batch
+    gradient, and both replicas take the same step."""
+    import pickle
+    import numpy as np
+    from oracle import fno_oracle
+    with tempfile.TemporaryDirectory() as d:
+        mp.spawn(_dp_worker, args=(2, _free_port(), d), nprocs=2, join=True)
+        got = pickle.load(open(os.path.join(d, "dp.pkl"), "rb"))
+    params, x, t, w = _dp_case()
+    _, g_full, _ = fno_oracle.loss_and_grads(params, x.numpy(), t.numpy(), weights_bf16=False, sample_w=w.numpy())
+    for rec in got:
+        assert np.allclose(rec["g"], g_full, rtol=1e-4, atol=1e-6 * np.abs(g_full).max())
+    assert np.array_equal(got[0]["p"], got[1]["p"])

@@ -67,3 +67,30 @@ def test_fno_adam_reduces_loss():
         net.adam(3e-3)
     l1 = float(net.backward(x, tgt.contiguous()).item())
     assert l1 < 0.2 * l0, (l0, l1)
+
+
+def test_fno_set_grads_feeds_adam():
+    """set_grads replaces the gradients AdamW uses: the last backward's own gradients
+    routed through it give the identical step; zero gradients leave the parameters
+    as they are (no weight decay).  This is the data-parallel training path."""
+    from optifax_gb300.surrogate import FNO, N_PARAMS, init_params
+    rng = np.random.default_rng(6)
+    L, B = 256, 2
+    p0 = init_params(2)
+    a = FNO(n_bins=L, max_batch=B, params=p0)
+    b = FNO(n_bins=L, max_batch=B, params=p0)
+    c = FNO(n_bins=L, max_batch=B, params=p0)
+    x = torch.from_numpy(rng.normal(size=(B, 6, L)).astype(np.float32)).to(a.dev)
+    tgt = (x[:, :4] * 0.3).contiguous()
+    a.backward(x, tgt)
+    a.adam(1e-3)
+    g = torch.empty(N_PARAMS, dtype=torch.float32, device=b.dev)
+    b.backward(x, tgt, grads=g)
+    b.set_grads(g)
+    b.adam(1e-3)
+    assert torch.equal(a.params(), b.params())
+    c.backward(x, tgt)
+    c.set_grads(torch.zeros(N_PARAMS, dtype=torch.float32, device=c.dev))
+    before = c.params().clone()
+    c.adam(1e-3)
+    assert torch.equal(before, c.params())
