@@ -70,9 +70,10 @@ def test_fno_adam_reduces_loss():
 
 
 def test_fno_set_grads_feeds_adam():
-    """set_grads replaces the gradients AdamW uses: the last backward's own gradients
-    routed through it give the identical step; zero gradients leave the parameters
-    as they are (no weight decay).  This is the data-parallel training path."""
+    """set_grads replaces the gradients AdamW uses: two networks whose own backwards
+    differ (split-K atomics make gradients differ in the last bits from run to run)
+    take the identical step once given the same gradient vector; zero gradients leave
+    the parameters as they are (no weight decay).  This is the data-parallel path."""
     from optifax_gb300.surrogate import FNO, N_PARAMS, init_params
     rng = np.random.default_rng(6)
     L, B = 256, 2
@@ -82,13 +83,15 @@ def test_fno_set_grads_feeds_adam():
     c = FNO(n_bins=L, max_batch=B, params=p0)
     x = torch.from_numpy(rng.normal(size=(B, 6, L)).astype(np.float32)).to(a.dev)
     tgt = (x[:, :4] * 0.3).contiguous()
-    a.backward(x, tgt)
+    g = torch.empty(N_PARAMS, dtype=torch.float32, device=a.dev)
+    a.backward(x, tgt, grads=g)
+    a.set_grads(g)
     a.adam(1e-3)
-    g = torch.empty(N_PARAMS, dtype=torch.float32, device=b.dev)
-    b.backward(x, tgt, grads=g)
+    b.backward(x, tgt)
     b.set_grads(g)
     b.adam(1e-3)
     assert torch.equal(a.params(), b.params())
+    assert not torch.equal(a.params(), torch.as_tensor(p0, dtype=torch.float32, device=a.dev))
     c.backward(x, tgt)
     c.set_grads(torch.zeros(N_PARAMS, dtype=torch.float32, device=c.dev))
     before = c.params().clone()
