@@ -318,7 +318,8 @@ def train(net: FNO, X: torch.Tensor, T: torch.Tensor, *, epochs: int = 40, batch
         if log:
             log(f"epoch {ep}: train {hist['train_loss'][-1]:.4e} val signal rel-L2 median "
                 f"{hist['val_signal_rel_l2'][-1]:.4e}")
-    torch.cuda.synchronize(net.dev)
+    if net.dev.type == "cuda":
+        torch.cuda.synchronize(net.dev)
     hist["seconds"] = time.perf_counter() - t0
     hist["steps"] = step_i
     ve = evaluate(net, X[vdev], T[vdev]).cpu()

@@ -61,11 +61,16 @@ class _OracleNet:
     """Stand-in for the GPU network with the FP64 oracle's gradients (CPU), for the
     data-parallel step's host logic: backward, set_grads and a plain gradient step."""
 
-    def __init__(self, params):
+    def __init__(self, params, max_batch=4):
         import numpy as np
         self.p = np.array(params, dtype=np.float64)
         self.grad = None
         self.dev = torch.device("cpu")
+        self.max_batch = max_batch
+
+    def forward(self, x):
+        from oracle import fno_oracle
+        return torch.from_numpy(fno_oracle.forward(self.p, x.numpy(), weights_bf16=False)[0].astype("float32"))
 
     def backward(self, x, target, grads=None, sample_w=None):
         from oracle import fno_oracle
@@ -126,3 +131,46 @@ def test_two_rank_data_parallel_surrogate_step():
     for rec in got:
         assert np.allclose(rec["g"], g_full, rtol=1e-4, atol=1e-6 * np.abs(g_full).max())
     assert np.array_equal(got[0]["p"], got[1]["p"])
+
+
+def _train_case():
+    import numpy as np
+    from optifax_gb300 import surrogate
+    g = np.random.default_rng(7)
+    X = torch.from_numpy(g.standard_normal((13, surrogate.CIN, 64)).astype("float32"))
+    T = torch.from_numpy((0.5 * g.standard_normal((13, surrogate.COUT, 64))).astype("float32"))
+    return surrogate.init_params(3), X, T
+
+
+def _train_worker(rank, world, port, out_dir):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    from optifax_gb300 import dist, fastforward
+    r, _, _ = dist.init("gloo")
+    params, X, T = _train_case()
+    net = _OracleNet(params)
+    fastforward.train(net, X, T, epochs=2, batch=4, lr=1e-3, val_frac=0.1, seed=3)
+    got = dist.gather_to_rank0(net.p)
+    dist.barrier()
+    if r == 0:
+        import pickle
+        with open(os.path.join(out_dir, "train.pkl"), "wb") as f:
+            pickle.dump(got, f)
+    torch.distributed.destroy_process_group()
+
+
+def test_two_rank_training_matches_one_rank():
+    """fastforward.train over 2 ranks (each a half of every minibatch, gradients
+    averaged) ends with identical replicas equal to the single-rank run."""
+    import pickle
+    import numpy as np
+    from optifax_gb300 import fastforward
+    with tempfile.TemporaryDirectory() as d:
+        mp.spawn(_train_worker, args=(2, _free_port(), d), nprocs=2, join=True)
+        got = pickle.load(open(os.path.join(d, "train.pkl"), "rb"))
+    params, X, T = _train_case()
+    one = _OracleNet(params)
+    fastforward.train(one, X, T, epochs=2, batch=4, lr=1e-3, val_frac=0.1, seed=3)
+    assert np.array_equal(got[0], got[1])
+    assert np.allclose(got[0], one.p, rtol=1e-5, atol=1e-7)
+    assert not np.allclose(one.p, params)
