@@ -68,3 +68,20 @@ def test_replay_reproduces_schedule():
     assert a.steps == b.steps
     assert np.array_equal(a.AT, b.AT)
     assert any(ok == 0 for _, ok in a.steps) or a.attempts == a.accepted
+
+
+def test_raman_term_is_the_causal_convolution():
+    """gnlsefib.m's RS = dT fR fft(ifft(|A|^2) RW), RW = n ifft(fftshift(hR)), is the
+    causal circular convolution dT fR sum_j hR(j dT) |A|^2_{l-j} (convolution theorem
+    with MATLAB's fft/ifft): the time origin and fftshift placement are right."""
+    n = 128
+    T = _grid(n, 2e-12)
+    rng = np.random.default_rng(3)
+    IT = rng.uniform(0.0, 2.0, n)
+    hR = go.raman_response(T)
+    ops = go.gnlse_ops(T, 0.0, 1.0, [0.0], 0.0, 0.18, hR)
+    RS = ops.dT * ops.fr * np.fft.fft(np.fft.ifft(IT) * ops.RW)
+    hs = np.fft.fftshift(hR)                          # hR(j dT) at index j (zero for t < 0)
+    direct = np.array([ops.dT * ops.fr * sum(hs[j] * IT[(l - j) % n] for j in range(n)) for l in range(n)])
+    assert np.max(np.abs(RS - direct)) <= 1e-12 * np.max(np.abs(direct))
+    assert np.all(hs[n // 2 + 1:] == 0.0)             # causal: nothing from the future
