@@ -12,7 +12,8 @@
 // steps clamped to land on the save points (no interpolation), and positions
 // as integers in units of length / 2^40 so that every dispersion phase B_k z is
 // a 64-bit fixed-point product (exact mod one turn; only the final angle goes
-// through FP32).  FP32 field arithmetic, FP64 norms and step control.
+// through FP32).  FP32 field arithmetic, norms reduced across the CTA in FP64
+// (per-thread partials of 16 modes in FP32), FP64 step control.
 //
 // Layout: the CTA's M/16 threads hold the spectral state y in registers, 16
 // modes each, in the FFT's bit-reversed slot order (slot s <-> mode bitrev(s));
@@ -38,31 +39,39 @@ __constant__ double kDpC[7] = {0.0, 1.0 / 5, 3.0 / 10, 4.0 / 5, 8.0 / 9, 1.0, 1.
 
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
-// Sums of three per-thread values over the CTA in FP64; every thread gets them.
+// Sums of two per-thread values over the CTA in FP64; every thread gets them.
 template <int T>
-__device__ __forceinline__ void block_sum3(double a, double b, double c, double* red, double (&out)[3]) {
+__device__ __forceinline__ void block_sum2(double a, double b, double* red, double (&out)[2]) {
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, o);
         b += __shfl_xor_sync(0xffffffffu, b, o);
-        c += __shfl_xor_sync(0xffffffffu, c, o);
     }
     const int t = threadIdx.x;
     __syncthreads();                       // red may still be read from the previous call
     if ((t & 31) == 0) {
-        red[3 * (t >> 5)] = a;
-        red[3 * (t >> 5) + 1] = b;
-        red[3 * (t >> 5) + 2] = c;
+        red[2 * (t >> 5)] = a;
+        red[2 * (t >> 5) + 1] = b;
     }
     __syncthreads();
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    double s0 = 0.0, s1 = 0.0;
 #pragma unroll 1
     for (int w = 0; w < T / 32; ++w) {     // fixed order: identical totals in every thread
-        s0 += red[3 * w];
-        s1 += red[3 * w + 1];
-        s2 += red[3 * w + 2];
+        s0 += red[2 * w];
+        s1 += red[2 * w + 1];
     }
-    out[0] = s0; out[1] = s1; out[2] = s2;
+    out[0] = s0; out[1] = s1;
+}
+
+// Squared norms of a thread's 16 modes: FP32 partial sums (16 terms, relative
+// error below 1e-6), widened once for the FP64 block reduction.  GB300's FP64
+// pipe is narrow, so per-mode FP64 conversions and adds cost a visible share of
+// the step.
+__device__ __forceinline__ double norm2_16(const float2 (&a)[16]) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) s = fmaf(a[j].x, a[j].x, fmaf(a[j].y, a[j].y, s));
+    return (double)s;
 }
 
 // Own 16 slots of stage array j in the global scratch (128 contiguous bytes)
@@ -283,16 +292,10 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
         }
         if (stage == 0) {
             // initial step: 0.8 rtol^(1/5) max(||y||, thr) / ||f||
-            double py = 0.0, pf = 0.0;
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                py += (double)(y[j].x * y[j].x + y[j].y * y[j].y);
-                pf += (double)(v[j].x * v[j].x + v[j].y * v[j].y);
-            }
-            double s3[3];
-            block_sum3<T>(py, pf, 0.0, red, s3);
-            ny = sqrt(s3[0]);
-            const double nf = sqrt(s3[1]);
+            double s2[2];
+            block_sum2<T>(norm2_16(y), norm2_16(v), red, s2);
+            ny = sqrt(s2[0]);
+            const double nf = sqrt(s2[1]);
             if (nf == 0.0) h = hmax;
             else {
                 double hh = (0.8 * pow(P.rtol, 0.2)) * fmax(ny, thr) / nf / unit;
@@ -309,15 +312,9 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
 #pragma unroll
         for (int j = 0; j < 16; ++j) ev[j] = make_float2(0.f, 0.f);
         combine<-1, 7>(ev, K, M, t, base, hz);
-        double pe = 0.0, pn = 0.0;
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            pe += (double)(ev[j].x * ev[j].x + ev[j].y * ev[j].y);
-            pn += (double)(ys[j].x * ys[j].x + ys[j].y * ys[j].y);
-        }
-        double s3[3];
-        block_sum3<T>(pe, pn, 0.0, red, s3);
-        const double errn = sqrt(s3[0]), nyn = sqrt(s3[1]);
+        double s2[2];
+        block_sum2<T>(norm2_16(ev), norm2_16(ys), red, s2);
+        const double errn = sqrt(s2[0]), nyn = sqrt(s2[1]);
         const double err = errn / fmax(fmax(ny, nyn), thr);
         const bool ok = err <= P.rtol;
         if (t == 0 && P.trace && attempts < P.trace_cap) {
@@ -326,7 +323,10 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
         }
         ++attempts;
         if (!isfinite(errn) || !isfinite(nyn)) { status |= OPTIFAX_PULSE_NAN; break; }
-        const double fac = err == 0.0 ? 5.0 : 0.8 * pow(P.rtol / err, 0.2);
+        // step factor 0.8 (RelTol/err)^(1/5): it only scales the next integer step, so FP32
+        // powf serves (an error ratio beyond FP32's range gives inf, clamped to 5 below)
+        const float errf = (float)err;
+        const double fac = errf == 0.f ? 5.0 : (double)(0.8f * powf((float)P.rtol / errf, 0.2f));
         if (ok) {
             ++accepted;
             zc += hc;
@@ -356,7 +356,7 @@ template <int M>
 cudaError_t launch_one(const GnlseDev* d, int n_pulses, const Twiddle* tw1, const Twiddle* tw2, cudaStream_t st) {
     constexpr int PADM = M + M / 16;
     const size_t smem = sizeof(float2) * 2 * PADM + (sizeof(uint64_t) + sizeof(float2) + sizeof(float)) * M +
-                        sizeof(double) * 3 * (M / 16 / 32 > 0 ? M / 16 / 32 : 1);
+                        sizeof(double) * 2 * (M / 16 / 32 > 0 ? M / 16 / 32 : 1);
     cudaError_t e = cudaFuncSetAttribute(gnlse_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     gnlse_kernel<M><<<n_pulses, M / 16, smem, st>>>(d, tw1, tw2);
