@@ -14,7 +14,13 @@
  * gpuArrays / CUDA float2.  Every call is ordered on the given CUDA stream
  * (NULL = legacy default stream) and returns before the work completes.
  * Functions return OPTIFAX_OK or an optifax_status code; they never abort.
- * A handle may be used by one host thread at a time.
+ * A handle may be used by one host thread at a time.  Its calls may go to
+ * different streams: the handle's device scratch (descriptors, exchange
+ * buffers, stage rows) is shared by its calls, so a call on another stream than
+ * the previous call's waits on the GPU until the previous call's work is done.
+ * Independent concurrent work takes one handle per stream.  Calls on a handle
+ * are not for CUDA stream capture (descriptors are staged from host memory and
+ * the first use of a grid size builds its tables synchronously).
  */
 #ifndef OPTIFAX_H
 #define OPTIFAX_H

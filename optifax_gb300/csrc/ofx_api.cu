@@ -37,6 +37,9 @@ struct optifax_context {
     size_t gnlse_desc_cap = 0;
     float2* d_gnlse_k = nullptr;
     size_t gnlse_k_cap = 0;                  // complex values
+    cudaEvent_t done_ev = nullptr;           // end of the last call's work on the GPU
+    cudaStream_t done_stream = nullptr;      // the stream that call ran on
+    bool done_pending = false;               // done_ev has been recorded
     std::string last_error;
 };
 
@@ -80,6 +83,23 @@ int fail(optifax_context* h, int code, const std::string& msg) {
 
 int cuda_fail(optifax_context* h, cudaError_t e, const char* what) {
     return fail(h, OPTIFAX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Every call stages its descriptors into, and runs on, device scratch owned by the
+// handle.  A call on another stream than the previous call's first waits for that
+// call's work (done_ev); calls on one stream are in stream order already.
+int order_after_previous(optifax_context* h, cudaStream_t st) {
+    if (!h->done_pending || h->done_stream == st) return OPTIFAX_OK;
+    cudaError_t e = cudaStreamWaitEvent(st, h->done_ev, 0);
+    return e == cudaSuccess ? OPTIFAX_OK : cuda_fail(h, e, "cudaStreamWaitEvent(previous call)");
+}
+
+int mark_done(optifax_context* h, cudaStream_t st) {
+    cudaError_t e = cudaEventRecord(h->done_ev, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord(end of call)");
+    h->done_pending = true;
+    h->done_stream = st;
+    return OPTIFAX_OK;
 }
 
 // W_n^e for e < count, built once per (n, count) map and kept for the context
@@ -245,13 +265,15 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         if (e != cudaSuccess) { h->desc_cap = 0; return cuda_fail(h, e, "cudaMalloc(descriptors)"); }
         h->desc_cap = cap;
     }
+    int rc = order_after_previous(h, st);
+    if (rc) return rc;
     cudaError_t e = cudaMemcpyAsync(h->d_desc, all.data(), nb, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(descriptors)");
     if (shared) {
         e = cudaMemsetAsync(h->d_grid_flags, 0, 4 * sizeof(int), st);
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync(grid flags)");
     }
-    int rc = ensure_sync_objects(h, groups.size());
+    rc = ensure_sync_objects(h, groups.size());
     if (rc) return rc;
     // tables first: building one synchronises the stream, which must not
     // happen between the launches
@@ -326,7 +348,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         }
         off += g.d.size();
     }
-    return OPTIFAX_OK;
+    return mark_done(h, st);
 }
 
 int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, int C, int method,
@@ -404,6 +426,8 @@ int optifax_create(optifax_handle* out, int device) {
     h->device = device;
     e = cudaMalloc(&h->d_grid_flags, 4 * sizeof(int));
     if (e != cudaSuccess) { delete h; return OPTIFAX_ERR_CUDA; }
+    e = cudaEventCreateWithFlags(&h->done_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) { cudaFree(h->d_grid_flags); delete h; return OPTIFAX_ERR_CUDA; }
     *out = h;
     return OPTIFAX_OK;
 }
@@ -422,6 +446,7 @@ int optifax_destroy(optifax_handle h) {
     if (h->d_gnlse_k) cudaFree(h->d_gnlse_k);
     for (auto s_ : h->side) cudaStreamDestroy(s_);
     for (auto e_ : h->ev) cudaEventDestroy(e_);
+    if (h->done_ev) cudaEventDestroy(h->done_ev);
     delete h;
     return OPTIFAX_OK;
 }
@@ -638,10 +663,12 @@ extern "C" int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses
         h->gnlse_desc_cap = (size_t)n_pulses;
     }
     for (int i = 0; i < n_pulses; ++i) d[(size_t)i].K = h->d_gnlse_k + (size_t)7 * M * i;
+    rc = order_after_previous(h, st);
+    if (rc) return rc;
     cudaError_t e = cudaMemcpyAsync(h->d_gnlse_desc, d.data(), sizeof(GnlseDev) * (size_t)n_pulses,
                                     cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(gnlse descriptors)");
     e = launch_gnlse(M, h->d_gnlse_desc, n_pulses, twp, twp + M, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "gnlse_kernel launch");
-    return OPTIFAX_OK;
+    return mark_done(h, st);
 }

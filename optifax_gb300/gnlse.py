@@ -20,7 +20,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .solver import context, _stream_ptr
+from .solver import context, _stream_ptr, on_stream
 
 GNLSE_POINTS = (512, 1024, 2048, 4096)
 
@@ -79,6 +79,7 @@ class GnlseRun:
     trace: Optional[torch.Tensor]  # (B, trace_cap, 2) int64: step (length/2^40 units), accepted
 
 
+@on_stream
 def propagate(ops: FibreOperators, A, flength: float, nsaves: int, *, w0: float = 0.0, rtol: float = 1e-5,
               atol: float = 1e-12, device: int = 0, trace_cap: int = 0, max_attempts: int = 0,
               stream=None) -> GnlseRun:

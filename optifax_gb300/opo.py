@@ -24,7 +24,7 @@ import torch
 
 from . import _native as nat
 from . import physics as ph
-from .solver import context, _stream_ptr
+from .solver import context, _stream_ptr, on_stream
 
 TALLY_OUTPUT, TALLY_OUTPUT_SIGNAL, TALLY_INTRACAVITY, TALLY_PUMP_BAND = range(4)
 ESD_OUTPUT, ESD_XTAL_OUT = range(2)
@@ -217,6 +217,7 @@ class OpticalSim:
                 "idler": np.where(lam_nm < 2 * pump_lim, 0.0, xt)}
 
 
+@on_stream
 def run_many(sims, n_trips: int, *, steady_tol: float = 0.0, steady_trips: int = 0,
              steady_tally: int = TALLY_OUTPUT_SIGNAL, stream=None, host_out: bool = True,
              history: bool = False, esd: bool = False, step_records: bool = False):

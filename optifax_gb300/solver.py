@@ -14,6 +14,7 @@ from __future__ import annotations
 
 import ctypes
 import dataclasses
+import functools
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -38,6 +39,24 @@ def _stream_ptr(stream) -> int:
     return int(stream.cuda_stream)
 
 
+def on_stream(fn):
+    """Run a wrapper taking ``stream=`` wholly on that stream: input preparation
+    (contiguous copies, zeroed records), the library call and any read-back.  The
+    given stream first waits for the current stream, where the caller made the
+    inputs; temporaries are then allocated on the given stream, so the caching
+    allocator cannot hand them out while the call still reads them.  Outputs are
+    ready on the given stream (synchronise it before using them elsewhere).
+    stream=None, or the current stream, runs the wrapper unchanged."""
+    @functools.wraps(fn)
+    def wrapper(*args, stream=None, **kw):
+        if stream is None or stream == torch.cuda.current_stream(stream.device):
+            return fn(*args, stream=stream, **kw)
+        stream.wait_stream(torch.cuda.current_stream(stream.device))
+        with torch.cuda.stream(stream):
+            return fn(*args, stream=stream, **kw)
+    return wrapper
+
+
 def _cuda(t, dtype):
     if not isinstance(t, torch.Tensor) or not t.is_cuda:
         raise TypeError("solver arrays must be CUDA tensors")
@@ -55,6 +74,7 @@ def n_chunks(n_steps: int, sel: float, variant: int = VARIANT_BATCH_XTAL) -> int
     return nc
 
 
+@on_stream
 def opo_mex_batch(Et, xT_h, G33, w0, bdiffw0, h, nSteps, dt, hBarg, maxErr, minErr, sel,
                   ApFT, stepMods, *, variant: int = VARIANT_BATCH_XTAL, stream=None):
     """[Et, ApFT, stepMods] = Solver(Et, T_step, G33, w0, bdiffw0, h, nSteps, dt, hB,
@@ -117,6 +137,7 @@ class PulseSpec:
     cta_points: int = 0                        # points per CTA (0: the call's choice / autotuned)
 
 
+@on_stream
 def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int = VARIANT_BATCH_XTAL,
               cta_points: int = 0, stream=None, want_stats: bool = True):
     """Run every pulse's crystal pass in one call; returns (outputs, stats array or None)."""
@@ -166,6 +187,7 @@ def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int =
     return [p.out for p in pulses], stats
 
 
+@on_stream
 def propagate_fp64(E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
                    variant: int = VARIANT_BATCH_XTAL, trace_cap: int = 0, stream=None):
     """The plain full-FP64 crystal pass (optifax_propagate_fp64).

@@ -80,3 +80,24 @@ def test_struct_layouts_match_ctypes(tmp_path):
         assert got[(cname, "size")] == ctypes.sizeof(cls), cname
         for f, _ in cls._fields_:
             assert got[(cname, f)] == getattr(cls, f).offset, (cname, f)
+
+
+def test_stream_wrapper_passes_through_without_a_stream():
+    """solver.on_stream leaves calls without a stream as they are (no CUDA use) and keeps
+    the wrapped function's name, signature checks and errors."""
+    import numpy as np
+    from optifax_gb300 import solver, gnlse, opo, _native as nat
+    calls = []
+
+    @solver.on_stream
+    def f(x, *, stream=None):
+        calls.append(stream)
+        return x + 1
+
+    assert f(1) == 2 and calls == [None] and f.__name__ == "f"
+    for fn in (solver.propagate, solver.opo_mex_batch, solver.propagate_fp64, opo.run_many, gnlse.propagate):
+        assert fn.__wrapped__ is not None
+    T = np.arange(-500, 500) * 1e-15
+    ops = gnlse.fibre_operators(T, 0.0, 0.11, [-1e-26], 0.0, 0.0, 0.0)
+    with pytest.raises(nat.OptifaxError):
+        gnlse.propagate(ops, np.ones(1000), 0.01, 3)
