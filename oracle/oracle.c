@@ -36,6 +36,13 @@
  * The FFT is a plain radix-2 FP64 transform of our own (FFTW, which MATLAB
  * uses, and cuFFT, which the MEX uses, are closed binaries and neither is
  * available here); any transform exact to FP64 rounding is equivalent.
+ *
+ * Threads: independent schedules (pulses) run in parallel.  A call with one
+ * schedule of 4096 points or more and an explicit thread count (nthreads > 0)
+ * spreads the pass's point loops and FFT butterflies over those threads
+ * instead; with nthreads = 0 a pass stays on one thread.  Each point's
+ * arithmetic is the same whichever thread does it and the only reductions (a
+ * max and an OR) are exact, so the results do not depend on the thread count.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -48,6 +55,17 @@
 #include "oracle.h"
 
 typedef struct { double re, im; } cplx;
+
+/* point loops of one schedule go parallel from this many points, when the
+ * calling thread runs a lone schedule with an explicit thread count (t_inner)
+ * and no outer (per-schedule) parallel region is active */
+#define OFX_PAR_MIN 4096
+#ifdef _OPENMP
+static _Thread_local int t_inner = 0;
+static inline int par_ok(size_t count) { return t_inner && count >= OFX_PAR_MIN && !omp_in_parallel(); }
+#else
+static inline int par_ok(size_t count) { (void)count; return 0; }
+#endif
 
 static inline cplx cmk(double r, double i) { cplx z = {r, i}; return z; }
 static inline cplx cadd(cplx a, cplx b) { return cmk(a.re + b.re, a.im + b.im); }
@@ -94,14 +112,21 @@ static void fft_plan_free(fft_plan* p) { free(p->tw); free(p->rev); }
 
 static void fft_exec(const fft_plan* p, cplx* x, int inverse) {
     const int n = p->n;
-    for (int i = 0; i < n; ++i) {
-        int r = p->rev[i];
-        if (r > i) { cplx t = x[i]; x[i] = x[r]; x[r] = t; }
-    }
-    for (int len = 2; len <= n; len <<= 1) {
-        int half = len >> 1, step = n / len;
-        for (int b = 0; b < n; b += len) {
-            for (int j = 0; j < half; ++j) {
+#pragma omp parallel if (par_ok((size_t)n))
+    {
+#pragma omp for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            int r = p->rev[i];
+            if (r > i) { cplx t = x[i]; x[i] = x[r]; x[r] = t; }
+        }
+        /* stage by stage (the implicit barrier of each loop), butterfly q of n/2:
+         * block (q / half) of length len, offset j = q mod half */
+        for (int len = 2; len <= n; len <<= 1) {
+            const int half = len >> 1, step = n / len;
+#pragma omp for schedule(static)
+            for (int q = 0; q < n / 2; ++q) {
+                const int j = q & (half - 1);
+                const int b = (q - j) << 1;
                 cplx w = p->tw[j * step];
                 if (inverse) w = cconj(w);
                 cplx u = x[b + j], v = cmul(x[b + j + half], w);
@@ -143,6 +168,7 @@ static double sample_time(int mode, int i, int n, double dt) {
 /* NL = A^2 e^{i phi} + 2 |A|^2 e^{-i phi},  phi = w0 t_i - bdwz
  * (OPO_CUDA_BATCH_XTAL.cu:182-187; NEE_CPU.m:98-101). */
 static void nl_eval(const cplx* A, cplx* NL, int n, const double* tw0, double bdwz) {
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
     for (int i = 0; i < n; ++i) {
         cplx e = cexpi(tw0[i] - bdwz);
         cplx a = A[i];
@@ -155,6 +181,7 @@ static void nl_eval(const cplx* A, cplx* NL, int n, const double* tw0, double bd
 /* K = -i h G (NL - i/(2 dt w0) (NL[i+1] - NL[i-1])), periodic neighbours
  * (OPO_CUDA_BATCH_XTAL.cu:221-249; NEE_CPU.m:103-105). */
 static void k_eval(const cplx* NL, cplx* K, int n, double hmod, double g, double c_shock) {
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
     for (int i = 0; i < n; ++i) {
         int ip = (i + 1 == n) ? 0 : i + 1;
         int im = (i == 0) ? n - 1 : i - 1;
@@ -269,6 +296,7 @@ static int classify(const sched_ctx* c, const cplx* E, const cplx* A1, double sc
     const ofx_oracle_params* p = c->p;
     int flags = 0; double pm = 0.0;
     size_t tot = (size_t)p->N * (size_t)c->nb;
+#pragma omp parallel for schedule(static) reduction(max : pm) reduction(| : flags) if (par_ok(tot))
     for (size_t i = 0; i < tot; ++i) {
         double ae = cabs2(E[i]);
         if (ae > 0) {
@@ -300,8 +328,10 @@ static void dispersion_step(sched_ctx* c, work* w, cplx* E, cplx* A0, int s, int
     double inv_n = 1.0 / (double)n;
     for (int b = 0; b < c->nb; ++b) {
         cplx* e = E + (size_t)b * n;
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
         for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_mex(p->abc_mode, i, n));
         fft_exec(&w->plan, e, 0);
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
         for (int i = 0; i < n; ++i) {
             cplx f = cscale(cexpi(-c->beta[i] * (double)s), pow(c->alpha[i], (double)s));
             e[i] = cmul(e[i], f);
@@ -313,6 +343,7 @@ static void dispersion_step(sched_ctx* c, work* w, cplx* E, cplx* A0, int s, int
         }
         fft_exec(&w->plan, e, 1);
         cplx* a0 = A0 + (size_t)b * n;
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
         for (int i = 0; i < n; ++i) a0[i] = cscale(e[i], inv_n);
     }
     if (c->stepmods && k < p->stepmods_limit && k < p->S && k >= 0) c->stepmods[k] = (double)s;
@@ -341,9 +372,11 @@ static void run_heun_mex(sched_ctx* c, work* w) {
             double hmod = stepmod * p->h;
             stage(c, w, w->A0, w->K1, k, hmod, kidx);
             size_t tot = (size_t)n * c->nb;
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i)
                 w->A1[i] = cadd(w->A0[i], cadd(cscale(w->K1[i], 0.5), cscale(w->K1[i], 0.5)));
             stage(c, w, w->A1, w->K2, k + stepmod, hmod, kidx);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i)
                 w->E[i] = cadd(w->A0[i], cadd(cscale(w->K2[i], 0.5), cscale(w->K1[i], 0.5)));
             int fl = classify(c, w->E, w->A1, 100.0, &pm);
@@ -396,6 +429,7 @@ static void run_rk23_mex(sched_ctx* c, work* w) {
     stepmod = stepprev;
     /* initial K1 at k = 0 (:432-438) */
     stage(c, w, w->A0, K1, k, stepmod * p->h, 0);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
     for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
     for (int chunk = 0; chunk < nchunks; ++chunk) {
         stepmod = stepprev;
@@ -404,13 +438,16 @@ static void run_rk23_mex(sched_ctx* c, work* w) {
             int kidx = (int)k;
             double hmod = stepmod * p->h;
             stage(c, w, w->A1, w->K2, k + 0.5 * stepmod, hmod, kidx);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(w->K2[i], 0.75));
             stage(c, w, w->A1, w->K3, k + 0.75 * stepmod, hmod, kidx);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i) {
                 cplx e = cadd(w->A0[i], cadd(cscale(w->K3[i], 4.0 / 9.0), cscale(w->K2[i], 1.0 / 3.0)));
                 w->E[i] = cadd(e, cscale(K1[i], 2.0 / 9.0));
             }
             stage(c, w, w->E, K4, k + stepmod, hmod, kidx);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i) {
                 cplx a = cadd(w->A0[i], cadd(cscale(K4[i], 1.0 / 8.0), cscale(w->K3[i], 1.0 / 3.0)));
                 a = cadd(a, cscale(w->K2[i], 1.0 / 4.0));
@@ -428,6 +465,7 @@ static void run_rk23_mex(sched_ctx* c, work* w) {
                 stepprev = stepmod;
                 /* K1 recomputed at the new start, G index k (:484-487) */
                 stage(c, w, w->A0, K1, k + stepmod, stepmod * p->h, (int)k);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
                 for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
             } else {
                 record(c, attempt, kidx, (int)stepmod, fl, 1);
@@ -435,6 +473,7 @@ static void run_rk23_mex(sched_ctx* c, work* w) {
                 c->stats->z_steps += (long long)stepmod;
                 dispersion_step(c, w, w->E, w->A0, (int)stepmod, chunk, nchunks, kidx);
                 cplx* t = K1; K1 = K4; K4 = t;     /* FSAL swap (:512-514) */
+#pragma omp parallel for schedule(static) if (par_ok(tot))
                 for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
                 if (k + stepmod >= cend && k < cend - 1.0) {
                     stepend = (cend - k) - 1.0;
@@ -469,17 +508,21 @@ static void run_heun_nee(sched_ctx* c, work* w) {
     for (int chunk = 1; chunk <= nchunks; ++chunk) {
         while (k < (double)chunk * p->sel && k <= (double)p->S) {
             int nan = 0;
+#pragma omp parallel for schedule(static) reduction(| : nan) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i) if (isnan(w->A0[i].re) || isnan(w->A0[i].im)) nan = 1;
             if (nan) { c->stats->status |= OFX_ORACLE_STATUS_NAN; break; }
             int kidx = (int)k - 1;                /* G33(k), 1-based */
             double hmod = p->h * stepmod;
             stage(c, w, w->A0, w->K1, k - 1.0, hmod, kidx);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i) w->A1[i] = cadd(w->A0[i], w->K1[i]);
             stage(c, w, w->A1, w->K2, k - 1.0 + stepmod, hmod, kidx);
+#pragma omp parallel for schedule(static) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i)
                 w->E[i] = cadd(cadd(w->A0[i], cscale(w->K1[i], 0.5)), cscale(w->K2[i], 0.5));
             /* pcterr = 100 max(|Et-A1|/(|Et|+1)) over all points */
             pm = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : pm) if (par_ok(tot))
             for (size_t i = 0; i < tot; ++i) {
                 double v = 100.0 * cabs2(csub(w->E[i], w->A1[i])) / (cabs2(w->E[i]) + 1.0);
                 if (v > pm) pm = v;
@@ -497,14 +540,17 @@ static void run_heun_nee(sched_ctx* c, work* w) {
                 c->stats->z_steps += (long long)stepmod;
                 for (int b = 0; b < c->nb; ++b) {
                     cplx* e = w->E + (size_t)b * n;
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
                     for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_nee(i, n, p->dt));
                     fft_exec(&w->plan, e, 0);
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
                     for (int i = 0; i < n; ++i) {
                         cplx f = cscale(cexpi(-c->beta[i] * stepmod), pow(c->alpha[i], stepmod));
                         e[i] = cmul(e[i], f);
                     }
                     fft_exec(&w->plan, e, 1);
                     cplx* a0 = w->A0 + (size_t)b * n;
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
                     for (int i = 0; i < n; ++i) a0[i] = cscale(e[i], 1.0 / (double)n);
                 }
                 if (!(fl & 2)) stepmod = stepmod + 1.0;     /* pcterr < minErr */
@@ -559,7 +605,8 @@ int ofx_oracle_run(const ofx_oracle_params* p,
     int rc_all = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel for schedule(dynamic, 1) reduction(| : rc_all)
+    t_inner = (nthreads > 1 && nsched == 1);
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : rc_all) if (nsched > 1)
 #endif
     for (int s = 0; s < nsched; ++s) {
         sched_ctx c;

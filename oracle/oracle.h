@@ -42,7 +42,11 @@ typedef struct {
  * trace: per schedule 3*trace_cap ints (k, stepmod, flags) where flags bit0 =
  * above maxErr, bit1 = above minErr, bit2 = NaN, bit3 = accepted.
  * forced_flags (optional): per schedule n_forced decisions replayed in place
- * of the computed ones (bits 0-1). stats: one per schedule. */
+ * of the computed ones (bits 0-1). stats: one per schedule.
+ * nthreads: 0 = OpenMP's default team over the schedules, each schedule on one
+ * thread; > 0 = that many threads, over the schedules when there are several,
+ * else inside the one pass (point loops and FFT stages, N >= 4096).  Results
+ * are bit-identical for every thread count. */
 int ofx_oracle_run(const ofx_oracle_params* p,
                    const double* E_in, const double* alpha, const double* G, const double* beta,
                    double* A_out, double* Ap, long long ap_len_complex, double* stepmods,

@@ -152,3 +152,16 @@ def test_undepleted_shg_follows_sinc(oracle):
     peak = k * 2 / c["delta"]
     dev = max(abs(sh - k * p) for sh, p in out) / peak
     assert dev < 1e-5, dev
+
+
+def test_threads_inside_one_pass_are_bit_identical(oracle):
+    """A lone 4096-point pass with an explicit thread count spreads its point loops and
+    FFT stages over the threads; every result bit is the same as on one thread."""
+    win, si, E = make_case(N=4096, length=0.03e-3, power=2.0)
+    kw = dict(w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps, dt=si.dt, max_err=si.max_err,
+              min_err=si.min_err, sel=si.sel, trace_cap=10000)
+    one = oracle.run(E, si.alpha, si.G, si.beta, nthreads=1, **kw)
+    many = oracle.run(E, si.alpha, si.G, si.beta, nthreads=3, **kw)
+    assert one.stats[0]["attempts"] > 10
+    assert np.array_equal(one.A, many.A) and np.array_equal(one.Ap, many.Ap)
+    assert np.array_equal(one.trace[0], many.trace[0])
