@@ -1,5 +1,5 @@
 """The reference-kernel harness (oracle/Makefile target `ref`) builds without a GPU:
-the driver library exports its entry points and, where the reference source is
+the harness library exports its entry points and, where the reference source is
 present, the five MEX kernel files compile unmodified into cubins."""
 import os
 import shutil
