@@ -645,6 +645,8 @@ extern "C" int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses
         g.n_saves = S;
     }
     cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t de = cudaSetDevice(h->device);
+    if (de != cudaSuccess) return cuda_fail(h, de, "cudaSetDevice");
     int rc = OPTIFAX_OK;
     const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
     if (!twp) return rc;
