@@ -38,7 +38,6 @@ struct optifax_context {
     float2* d_gnlse_k = nullptr;
     size_t gnlse_k_cap = 0;                  // complex values
     cudaEvent_t done_ev = nullptr;           // end of the last call's work on the GPU
-    cudaStream_t done_stream = nullptr;      // the stream that call ran on
     bool done_pending = false;               // done_ev has been recorded
     std::string last_error;
 };
@@ -86,10 +85,11 @@ int cuda_fail(optifax_context* h, cudaError_t e, const char* what) {
 }
 
 // Every call stages its descriptors into, and runs on, device scratch owned by the
-// handle.  A call on another stream than the previous call's first waits for that
-// call's work (done_ev); calls on one stream are in stream order already.
+// handle, so its work waits for the previous call's (done_ev).  On the previous
+// call's own stream the wait adds nothing to stream order; it is made on every
+// stream because a stream handle's value can be reused after the stream is destroyed.
 int order_after_previous(optifax_context* h, cudaStream_t st) {
-    if (!h->done_pending || h->done_stream == st) return OPTIFAX_OK;
+    if (!h->done_pending) return OPTIFAX_OK;
     cudaError_t e = cudaStreamWaitEvent(st, h->done_ev, 0);
     return e == cudaSuccess ? OPTIFAX_OK : cuda_fail(h, e, "cudaStreamWaitEvent(previous call)");
 }
@@ -98,7 +98,6 @@ int mark_done(optifax_context* h, cudaStream_t st) {
     cudaError_t e = cudaEventRecord(h->done_ev, st);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord(end of call)");
     h->done_pending = true;
-    h->done_stream = st;
     return OPTIFAX_OK;
 }
 
