@@ -248,13 +248,6 @@ def encode_pairs(ins: torch.Tensor, outs: torch.Tensor, crop, chunk: int = 1024)
     return torch.cat(xs), torch.cat(ts)
 
 
-def generate_pairs(specs: List[opo.CavitySpec], n_trips: int, crop, device: int = 0, group: int = 38):
-    """generate_raw + encode_pairs: (x, target, trip index, solver attempts)."""
-    ins, outs, trip_idx, attempts = generate_raw(specs, n_trips, device, group)
-    X, T = encode_pairs(ins, outs, crop)
-    return X, T, trip_idx, attempts
-
-
 def signal_rel_err(y: torch.Tensor, t: torch.Tensor) -> torch.Tensor:
     """Per-sample relative L2 error of the signal channels (2, 3)."""
     d = (y[:, 2:4] - t[:, 2:4]).flatten(1).norm(dim=1)
