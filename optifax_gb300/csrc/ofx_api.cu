@@ -319,8 +319,7 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
             e = cudaStreamWaitEvent(ls, h->ev[0], 0);
             if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamWaitEvent(fork)");
         }
-        cudaLaunchConfig_t lc;
-        memset(&lc, 0, sizeof(lc));
+        cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3((unsigned)(g.d.size() * C), 1, 1);
         lc.blockDim = dim3(M / 16, 1, 1);
         lc.dynamicSmemBytes = ke->smem;

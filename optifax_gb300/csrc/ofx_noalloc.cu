@@ -196,8 +196,7 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
     tabs.tw2 = tabs.tw1 + kM;
     tabs.quad = reinterpret_cast<const Twiddle*>(base + kOffQuad);
     tabs.low = reinterpret_cast<const Twiddle*>(base + kOffN);
-    cudaLaunchConfig_t lc;
-    memset(&lc, 0, sizeof(lc));
+    cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)C, 1, 1);
     lc.blockDim = dim3(kM / 16, 1, 1);
     lc.dynamicSmemBytes = ke->smem;
