@@ -23,6 +23,24 @@ def test_partition_balances_and_covers():
     assert [len(p) for p in dist.partition_by_cost([1.0], 2)] in ([1, 0], [0, 1])
 
 
+def test_partition_invariants_on_random_costs():
+    """Heavy-tailed random costs, 0-59 instances, 1-11 ranks: contiguous ranges in rank
+    order covering every instance once, and every boundary within one instance of its
+    target, so no rank carries more than total / world + 2 max(cost)."""
+    import numpy as np
+    from optifax_gb300 import dist
+    rng = np.random.default_rng(0)
+    for _ in range(2000):
+        n, world = int(rng.integers(0, 60)), int(rng.integers(1, 12))
+        costs = list(rng.pareto(1.5, size=n) + 0.01)
+        parts = dist.partition_by_cost(costs, world)
+        assert len(parts) == world
+        assert [i for p in parts for i in p] == list(range(n))
+        if n:
+            bound = sum(costs) / world + 2 * max(costs)
+            assert max(sum(costs[i] for i in p) for p in parts) <= bound + 1e-9
+
+
 def _worker(rank, world, port, out_dir):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
                       LOCAL_RANK=str(rank))
