@@ -85,3 +85,16 @@ def test_raman_term_is_the_causal_convolution():
     direct = np.array([ops.dT * ops.fr * sum(hs[j] * IT[(l - j) % n] for j in range(n)) for l in range(n)])
     assert np.max(np.abs(RS - direct)) <= 1e-12 * np.max(np.abs(direct))
     assert np.all(hs[n // 2 + 1:] == 0.0)             # causal: nothing from the future
+
+
+def test_pure_self_phase_modulation_is_exact():
+    """No dispersion, no Raman response, no shock term (w0 = 0): dA/dz = i gamma |A|^2 A
+    keeps |A| and turns the phase by gamma |A|^2 z at every instant."""
+    n = 512
+    T = _grid(n, 2e-12)
+    A = np.sqrt(1000.0) / np.cosh(T / 50e-15)
+    ops = go.gnlse_ops(T, 0.0, 0.11, [0.0], 0.0, 0.0, 0.0)
+    r = go.propagate(ops, A, 0.01, 3)
+    for i, z in enumerate(r.Z):
+        exact = A * np.exp(1j * 0.11 * np.abs(A) ** 2 * z)
+        assert np.linalg.norm(r.AT[i] - exact) / np.linalg.norm(exact) < 1e-6
