@@ -50,6 +50,20 @@ def test_gnlse_soliton_gpu():
     assert abs(ph - expect) < 1e-4
 
 
+def test_gnlse_pure_self_phase_modulation_gpu():
+    """No dispersion, Raman response or shock term: |A| is kept and the phase turns by
+    gamma |A|^2 z at every instant (FP32 field: 1e-5)."""
+    n = 512
+    T = _grid(n, 2e-12)
+    A = np.sqrt(1000.0) / np.cosh(T / 50e-15)
+    r, st, _ = _run_gpu(T, A, 0.0, [0.0], 0.0, 0.0, 0.0, 0.01, 3)
+    assert st["status"] == 0
+    AT = r.AT[0].cpu().numpy().astype(np.complex128)
+    for i, z in enumerate(r.Z):
+        exact = A * np.exp(1j * GAMMA * np.abs(A) ** 2 * z)
+        assert np.linalg.norm(AT[i] - exact) / np.linalg.norm(exact) < 1e-5
+
+
 @pytest.mark.parametrize("n,window,loss,L", [(512, 1.5e-12, 0.0, 0.01), (1024, 2e-12, 0.0, 0.01),
                                             (2048, 4e-12, 0.5, 0.01), (4096, 8e-12, 0.0, 0.01),
                                             (2048, 4e-12, 0.0, 0.08)])
