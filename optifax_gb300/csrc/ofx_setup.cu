@@ -34,7 +34,7 @@ __device__ double n_mgoln_e(double lam_um, double celsius) {
     const double n2 = (5.756 + 2.860e-6 * fn) + (0.0983 + 4.700e-8 * fn) / (l2 - a3 * a3) +
                       (189.32 + 1.516e-4 * fn) / (l2 - 12.52 * 12.52) - 1.32e-2 * l2;
     double n = n2 > 0.0 ? sqrt(n2) : 0.0;
-    if (!isfinite(n) || n < 1.0) n = 1.0;   // Dielectric.m:316-317
+    if (!isfinite(n) || n < 1.0) n = 1.0;   // Dielectric.m:43-44
     return n;
 }
 

@@ -20,7 +20,7 @@ reference's set-up arithmetic:
 Choices that the reference leaves to data files or does not define are
 stated where they are made: crystal transmission (lossless inside the
 simulation window's spectral limits, zero outside, which is what
-``transmission.m:166`` does at the limits), air index 1, and the one-photon-
+``transmission.m:28`` does at the limits), air index 1, and the one-photon-
 per-mode noise seed (the reference starts the intracavity field at zero).
 """
 from __future__ import annotations
@@ -113,7 +113,7 @@ def n_mgoln_e(lam_um: np.ndarray, celsius: float = 20.0) -> np.ndarray:
               + (g["a4"] + g["b4"] * fn) / (l2 - g["a5"] ** 2) - g["a6"] * l2)
     n = np.sqrt(n2.astype(np.complex128)).real
     n = np.where(np.isfinite(n), n, 1.0)
-    n[n < 1] = 1.0                 # Dielectric.m:316-317
+    n[n < 1] = 1.0                 # Dielectric.m:43-44
     return n
 
 
@@ -250,7 +250,7 @@ class Crystal:
 
 
 def window_transmission(win: SimWindow) -> np.ndarray:
-    """Lossless inside the window's spectral limits, zero outside (transmission.m:166)."""
+    """Lossless inside the window's spectral limits, zero outside (transmission.m:28)."""
     lam = win.wavelengths
     lo, hi = win.spectral_limits_nm
     t = ((lam >= lo * 1e-9) & (lam <= hi * 1e-9)).astype(np.float64)
