@@ -1,6 +1,8 @@
 """TEST INFRASTRUCTURE ONLY: FP64 restatement of the chi(3) fibre GNLSE solver
 (toolbox/lib/internal/main/gnlsefib.m) -- the oracle for optifax_gb300's GPU
-kernel in csrc/ofx_gnlse.cu.  Only tests/ import it.
+kernel in csrc/ofx_gnlse.cu.  Only tests/ and bench.py's cpu_baseline leg import
+it.  propagate_c binds the C restatement of the same scheme (oracle/gnlse_oracle.c),
+which runs independent pulses in parallel.
 
 The equation, grids and operators follow gnlsefib.m:22-66: the interaction-picture
 spectral field AW obeys dAW/dz = i gamma W ifft(AT ((1 - fR) |AT|^2 + RS)) e^{-Lz},
@@ -23,6 +25,7 @@ ODE to the same tolerance.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from dataclasses import dataclass
 
@@ -178,3 +181,58 @@ def propagate(ops: GnlseOps, A, flength, nsaves, rtol=1e-5, atol=1e-12, forced=N
         save(si, zc, y)
     Z = np.array([s * unit for s in saves])
     return GnlseResult(Z=Z, AT=out_at, AW=out_aw, steps=steps, attempts=att, accepted=acc)
+
+
+class _CParams(ctypes.Structure):
+    """ofx_gnlse_params (oracle/gnlse_oracle.h)."""
+    _fields_ = [("n", ctypes.c_int), ("n_saves", ctypes.c_int), ("gamma", ctypes.c_double),
+                ("fr", ctypes.c_double), ("dT", ctypes.c_double), ("alpha", ctypes.c_double),
+                ("length", ctypes.c_double), ("rtol", ctypes.c_double), ("atol", ctypes.c_double)]
+
+
+def propagate_c(ops: GnlseOps, A, flength, nsaves, rtol=1e-5, atol=1e-12, forced=None, nthreads=0,
+                trace_cap=200000):
+    """The C restatement (oracle/gnlse_oracle.c) of propagate() for a batch of fields
+    A (B x n, or n) in parallel; forced: per pulse a sequence of (h_count, accepted),
+    or one sequence for a single pulse.  Returns one GnlseResult per pulse."""
+    from . import oracle as orc
+    lib = orc.lib()
+    A = np.ascontiguousarray(np.atleast_2d(np.asarray(A, dtype=np.complex128)))
+    nb, n = A.shape
+    if n != ops.n:
+        raise ValueError("fields must have the operators' grid size")
+    p = _CParams(n=n, n_saves=int(nsaves), gamma=ops.gamma, fr=ops.fr if ops.raman else 0.0, dT=ops.dT,
+                 alpha=ops.alpha, length=float(flength), rtol=float(rtol), atol=float(atol))
+    B = np.ascontiguousarray(ops.B, dtype=np.float64)
+    W = np.ascontiguousarray(ops.W, dtype=np.float64)
+    RW = np.ascontiguousarray(ops.RW, dtype=np.complex128) if ops.raman else None
+    AT = np.zeros((nb, nsaves, n), dtype=np.complex128)
+    AW = np.zeros((nb, nsaves, n), dtype=np.complex128)
+    trace = np.zeros((nb, max(trace_cap, 1), 2), dtype=np.int64)
+    n_forced = 0
+    fz = None
+    if forced is not None:
+        fl = [forced] if nb == 1 and len(forced) and np.ndim(forced[0]) == 1 else list(forced)
+        n_forced = max(len(f) for f in fl)
+        fz = np.zeros((nb, max(n_forced, 1), 2), dtype=np.int64)
+        for b, f in enumerate(fl):
+            fz[b, :len(f)] = np.asarray(f, dtype=np.int64).reshape(-1, 2)
+    att = np.zeros(nb, dtype=np.int32)
+    acc = np.zeros(nb, dtype=np.int32)
+    dp = lambda a: a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+    fn = lib.ofx_gnlse_oracle_run
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(_CParams), ctypes.c_int] + [ctypes.c_void_p] * 7 + \
+        [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    rc = fn(ctypes.byref(p), nb, dp(A), dp(B), dp(W), dp(RW), dp(AT), dp(AW), dp(trace), trace_cap,
+            dp(fz), n_forced, dp(att), dp(acc), int(nthreads))
+    if rc != 0:
+        raise RuntimeError(f"ofx_gnlse_oracle_run failed ({rc})")
+    total = 1 << Z_BITS
+    Z = np.array([((i * total + (nsaves - 1) // 2) // (nsaves - 1)) * (flength / total) for i in range(nsaves)])
+    out = []
+    for b in range(nb):
+        k = min(int(att[b]), trace_cap)
+        steps = [(int(h), int(a)) for h, a in trace[b, :k]]
+        out.append(GnlseResult(Z=Z, AT=AT[b], AW=AW[b], steps=steps, attempts=int(att[b]), accepted=int(acc[b])))
+    return out

@@ -1,0 +1,99 @@
+/*
+ * oracle_fft.h -- TEST INFRASTRUCTURE ONLY.  FP64 complex helpers and the
+ * iterative radix-2 FFT shared by the CPU oracles (oracle.c: the chi(2) crystal
+ * pass; gnlse_oracle.c: the chi(3) fibre).  Unnormalised, sign -1 forward, +1
+ * inverse.  Every definition is static, so each oracle file has its own copy.
+ */
+#ifndef OFX_ORACLE_FFT_H
+#define OFX_ORACLE_FFT_H
+
+#include <math.h>
+#include <stdlib.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct { double re, im; } cplx;
+
+/* point loops of one schedule go parallel from this many points, when the
+ * calling thread runs a lone schedule with an explicit thread count (t_inner)
+ * and no outer (per-schedule) parallel region is active */
+#define OFX_PAR_MIN 4096
+#ifdef _OPENMP
+static _Thread_local int t_inner = 0;
+static inline int par_ok(size_t count) { return t_inner && count >= OFX_PAR_MIN && !omp_in_parallel(); }
+#else
+static inline int par_ok(size_t count) { (void)count; return 0; }
+#endif
+
+static inline cplx cmk(double r, double i) { cplx z = {r, i}; return z; }
+static inline cplx cadd(cplx a, cplx b) { return cmk(a.re + b.re, a.im + b.im); }
+static inline cplx csub(cplx a, cplx b) { return cmk(a.re - b.re, a.im - b.im); }
+static inline cplx cmul(cplx a, cplx b) {
+    return cmk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+static inline cplx cscale(cplx a, double s) { return cmk(a.re * s, a.im * s); }
+static inline cplx cconj(cplx a) { return cmk(a.re, -a.im); }
+static inline double cabs2(cplx a) { return hypot(a.re, a.im); }
+static inline cplx cexpi(double phi) { return cmk(cos(phi), sin(phi)); }
+
+/* ------------------------------------------------------------------------ */
+/* FFT: iterative radix-2, in place, unnormalised, sign -1 forward.          */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int n, log2n;
+    cplx* tw;       /* exp(-2 pi i e / n), e in [0, n/2) */
+    int* rev;       /* bit reversal permutation */
+} fft_plan;
+
+static int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
+
+static int fft_plan_init(fft_plan* p, int n) {
+    p->n = n; p->log2n = ilog2(n);
+    if ((1 << p->log2n) != n) return -1;
+    p->tw = (cplx*)malloc(sizeof(cplx) * (size_t)(n / 2 + 1));
+    p->rev = (int*)malloc(sizeof(int) * (size_t)n);
+    if (!p->tw || !p->rev) return -2;
+    for (int e = 0; e < n / 2; ++e) {
+        /* angle in turns computed exactly, then to radians */
+        double a = -2.0 * M_PI * (double)e / (double)n;
+        p->tw[e] = cmk(cos(a), sin(a));
+    }
+    for (int i = 0; i < n; ++i) {
+        int r = 0;
+        for (int b = 0; b < p->log2n; ++b) if (i & (1 << b)) r |= 1 << (p->log2n - 1 - b);
+        p->rev[i] = r;
+    }
+    return 0;
+}
+
+static void fft_plan_free(fft_plan* p) { free(p->tw); free(p->rev); }
+
+static void fft_exec(const fft_plan* p, cplx* x, int inverse) {
+    const int n = p->n;
+#pragma omp parallel if (par_ok((size_t)n))
+    {
+#pragma omp for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            int r = p->rev[i];
+            if (r > i) { cplx t = x[i]; x[i] = x[r]; x[r] = t; }
+        }
+        /* stage by stage (the implicit barrier of each loop), butterfly q of n/2:
+         * block (q / half) of length len, offset j = q mod half */
+        for (int len = 2; len <= n; len <<= 1) {
+            const int half = len >> 1, step = n / len;
+#pragma omp for schedule(static)
+            for (int q = 0; q < n / 2; ++q) {
+                const int j = q & (half - 1);
+                const int b = (q - j) << 1;
+                cplx w = p->tw[j * step];
+                if (inverse) w = cconj(w);
+                cplx u = x[b + j], v = cmul(x[b + j + half], w);
+                x[b + j] = cadd(u, v);
+                x[b + j + half] = csub(u, v);
+            }
+        }
+    }
+}
+
+#endif

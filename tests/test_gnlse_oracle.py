@@ -98,3 +98,39 @@ def test_pure_self_phase_modulation_is_exact():
     for i, z in enumerate(r.Z):
         exact = A * np.exp(1j * 0.11 * np.abs(A) ** 2 * z)
         assert np.linalg.norm(r.AT[i] - exact) / np.linalg.norm(exact) < 1e-6
+
+
+@pytest.mark.parametrize("n,loss,raman,shock", [(1024, 0.0, True, True), (2048, 0.5, True, True),
+                                               (512, 0.0, False, False)])
+def test_c_restatement_matches_numpy(n, loss, raman, shock):
+    """oracle/gnlse_oracle.c against this file's propagate(): the same step schedule and
+    fields to FP64 rounding (the FFTs differ), also when replaying a forced schedule."""
+    T = _grid(n, 2e-12 * n / 1024)
+    w0 = 2 * np.pi * 299792458.0 / 835e-9 if shock else 0.0
+    RT = go.raman_response(T) if raman else 0.0
+    ops = go.gnlse_ops(T, w0, 0.11, [-1.183e-26, 8.1e-41, -9.5e-56], loss, 0.18 if raman else 0.0, RT)
+    A = np.sqrt(1000.0) / np.cosh(T / 28.4e-15)
+    ref = go.propagate(ops, A, 0.01, 4)
+    own = go.propagate_c(ops, A, 0.01, 4)[0]
+    rep = go.propagate_c(ops, A, 0.01, 4, forced=ref.steps)[0]
+    assert own.steps == ref.steps and own.attempts == ref.attempts and own.accepted == ref.accepted
+    assert np.allclose(own.Z, ref.Z, rtol=0, atol=0)
+    for r in (own, rep):
+        for i in range(4):
+            assert np.linalg.norm(r.AT[i] - ref.AT[i]) <= 1e-12 * np.linalg.norm(ref.AT[i])
+            assert np.linalg.norm(r.AW[i] - ref.AW[i]) <= 1e-12 * np.linalg.norm(ref.AW[i])
+
+
+def test_c_restatement_batch_in_parallel_equals_one_by_one():
+    n = 512
+    T = _grid(n, 1.5e-12)
+    w0 = 2 * np.pi * 299792458.0 / 835e-9
+    ops = go.gnlse_ops(T, w0, 0.11, [-1.183e-26, 8.1e-41], 0.0, 0.18, go.raman_response(T))
+    A = np.stack([np.sqrt(p) / np.cosh(T / 28.4e-15) for p in (300.0, 900.0, 2000.0)])
+    batch = go.propagate_c(ops, A, 0.01, 3, nthreads=3)
+    for b in range(3):
+        one = go.propagate_c(ops, A[b], 0.01, 3, nthreads=1)[0]
+        assert batch[b].steps == one.steps
+        assert np.array_equal(batch[b].AT, one.AT) and np.array_equal(batch[b].AW, one.AW)
+    with pytest.raises(RuntimeError):                                     # forced schedule runs out
+        go.propagate_c(ops, A[0], 0.01, 3, forced=batch[0].steps[:2])
