@@ -43,6 +43,7 @@ static inline cplx cexpi(double phi) { return cmk(cos(phi), sin(phi)); }
 typedef struct {
     int n, log2n;
     cplx* tw;       /* exp(-2 pi i e / n), e in [0, n/2) */
+    cplx* tws;      /* the same values per stage, contiguous: stage len holds tw[j n / len], j < len / 2 */
     int* rev;       /* bit reversal permutation */
 } fft_plan;
 
@@ -52,12 +53,18 @@ static int fft_plan_init(fft_plan* p, int n) {
     p->n = n; p->log2n = ilog2(n);
     if ((1 << p->log2n) != n) return -1;
     p->tw = (cplx*)malloc(sizeof(cplx) * (size_t)(n / 2 + 1));
+    p->tws = (cplx*)malloc(sizeof(cplx) * (size_t)n);
     p->rev = (int*)malloc(sizeof(int) * (size_t)n);
-    if (!p->tw || !p->rev) return -2;
+    if (!p->tw || !p->tws || !p->rev) return -2;
     for (int e = 0; e < n / 2; ++e) {
         /* angle in turns computed exactly, then to radians */
         double a = -2.0 * M_PI * (double)e / (double)n;
         p->tw[e] = cmk(cos(a), sin(a));
+    }
+    size_t off = 0;
+    for (int len = 2; len <= n; len <<= 1) {
+        for (int j = 0; j < len / 2; ++j) p->tws[off + j] = p->tw[j * (n / len)];
+        off += (size_t)(len / 2);
     }
     for (int i = 0; i < n; ++i) {
         int r = 0;
@@ -67,11 +74,35 @@ static int fft_plan_init(fft_plan* p, int n) {
     return 0;
 }
 
-static void fft_plan_free(fft_plan* p) { free(p->tw); free(p->rev); }
+static void fft_plan_free(fft_plan* p) { free(p->tw); free(p->tws); free(p->rev); }
 
 static void fft_exec(const fft_plan* p, cplx* x, int inverse) {
     const int n = p->n;
-#pragma omp parallel if (par_ok((size_t)n))
+    if (!par_ok((size_t)n)) {
+        /* one thread: the same butterflies in the same order, block by block */
+        for (int i = 0; i < n; ++i) {
+            int r = p->rev[i];
+            if (r > i) { cplx t = x[i]; x[i] = x[r]; x[r] = t; }
+        }
+        const cplx* tw = p->tws;
+        for (int len = 2; len <= n; len <<= 1) {
+            const int half = len >> 1;
+            for (int b = 0; b < n; b += len) {
+                cplx* xa = x + b;
+                cplx* xb = x + b + half;
+                for (int j = 0; j < half; ++j) {
+                    cplx w = tw[j];
+                    if (inverse) w = cconj(w);
+                    cplx u = xa[j], v = cmul(xb[j], w);
+                    xa[j] = cadd(u, v);
+                    xb[j] = csub(u, v);
+                }
+            }
+            tw += half;
+        }
+        return;
+    }
+#pragma omp parallel
     {
 #pragma omp for schedule(static)
         for (int i = 0; i < n; ++i) {
