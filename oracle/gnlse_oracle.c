@@ -33,6 +33,7 @@
 #include "oracle_fft.h"
 
 #define Z_BITS 40
+#define MAX_ATTEMPTS 10000000
 
 /* Dormand-Prince 5(4) tableau (Dormand & Prince 1980); row 6 = the 5th-order
  * weights (FSAL), DP_E = b - b_hat */
@@ -167,7 +168,7 @@ static int run_one(const ofx_gnlse_params* p, const cplx* A, const double* B, co
     if (nf == 0.0) h = hmax;
     else {
         const double hh = (0.8 * pow(p->rtol, 0.2)) * fmax(ny, thr) / nf / unit;
-        h = hh >= (double)hmax ? hmax : ((long long)hh < 1 ? 1 : (long long)hh);
+        h = !(hh < (double)hmax) ? hmax : (hh < 1.0 ? 1 : (long long)hh);   /* NaN: hmax */
     }
     int att = 0, acc = 0, fi = 0;
     for (int si = 1; si < p->n_saves && rc == 0; ++si) {
@@ -202,6 +203,7 @@ static int run_one(const ofx_gnlse_params* p, const cplx* A, const double* B, co
             }
             const double nyn = norm(w.ynew, n);
             const double err = norm(w.acc, n) / fmax(fmax(ny, nyn), thr);
+            if (!isfinite(err) || att >= MAX_ATTEMPTS) { rc = isfinite(err) ? -5 : -4; break; }
             int ok = err <= p->rtol;
             if (forced) { ok = forced[2 * fi + 1] != 0; ++fi; }
             if (trace && att < trace_cap) { trace[2 * att] = hc; trace[2 * att + 1] = ok; }

@@ -29,7 +29,8 @@ typedef struct {
  * length / 2^40, accepted).  forced (optional): per pulse n_forced such pairs
  * replayed in place of the step control.  attempts, accepted: per pulse.
  * Returns 0, or -1 for bad arguments / -2 when memory runs out / -3 when a forced
- * schedule ends before the fibre does. */
+ * schedule ends before the fibre does / -4 when the error norm is not finite / -5
+ * after 10^7 attempts. */
 int ofx_gnlse_oracle_run(const ofx_gnlse_params* p, int n_pulses, const double* A, const double* B,
                          const double* W, const double* RW, double* AT_out, double* AW_out,
                          long long* trace, int trace_cap, const long long* forced, int n_forced,

@@ -50,6 +50,8 @@ typedef struct {
 static int ilog2(int n) { int l = 0; while ((1 << l) < n) ++l; return l; }
 
 static int fft_plan_init(fft_plan* p, int n) {
+    p->tw = p->tws = NULL;
+    p->rev = NULL;                      /* a failed init leaves nothing to free */
     p->n = n; p->log2n = ilog2(n);
     if ((1 << p->log2n) != n) return -1;
     p->tw = (cplx*)malloc(sizeof(cplx) * (size_t)(n / 2 + 1));

@@ -22,6 +22,8 @@ def test_fft_matches_numpy(oracle):
         x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
         assert np.max(np.abs(oracle.fft(x) - np.fft.fft(x))) < 1e-12 * n
         assert np.max(np.abs(oracle.fft(x, inverse=True) - np.fft.ifft(x) * n)) < 1e-12 * n
+    with pytest.raises(ValueError):                 # not a power of two: an error, nothing freed
+        oracle.fft(np.ones(1000, dtype=complex))
 
 
 def test_pure_dispersion_is_exact(oracle):
