@@ -1,4 +1,4 @@
-"""Fast-forward crop geometry (CPU)."""
+"""Fast-forward crop geometry, envelope resampling and host helpers (CPU)."""
 import numpy as np
 
 
@@ -34,3 +34,37 @@ def test_envelope_bands_abut_and_hold_the_feedback_band():
     assert int(np.argmax(np.abs(a.pump))) in {(kp + o) % N for o in range(lop, hip)}
     e = ff.envelope(a.pump, kp, lop, hip, crop.n_bins)
     assert abs(np.max(np.abs(e)) - crop.pump_scale) <= 1e-6 * crop.pump_scale
+
+
+def test_envelope_is_an_exact_resampling_of_its_band():
+    """envelope() places the band's bins on an n_bins grid and inverse-transforms them:
+    the transform of the envelope gives the band's bins back exactly, and nothing else."""
+    from optifax_gb300 import fastforward as ff
+    rng = np.random.default_rng(0)
+    N, L, kc, lo, hi = 4096, 256, 1000, -40, 90
+    X = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    e = ff.envelope(X, kc, lo, hi, L)
+    b = np.fft.fft(e) / L
+    o = np.arange(lo, hi)
+    assert np.allclose(b[o % L], X[(kc + o) % N], rtol=0, atol=1e-12)
+    rest = np.ones(L, bool)
+    rest[o % L] = False
+    assert np.max(np.abs(b[rest])) < 1e-12
+
+
+def test_interaction_picture_and_error_helpers():
+    import torch
+    from optifax_gb300 import fastforward as ff
+    rng = np.random.default_rng(1)
+    D = torch.from_numpy(np.exp(1j * rng.uniform(0, 6, 64)) * rng.uniform(0.5, 1.0, 64))
+    D[5] = 0
+    X = torch.from_numpy(rng.standard_normal(64) + 1j * rng.standard_normal(64))
+    Y = ff.to_interaction(X * D, D)
+    keep = torch.ones(64, dtype=torch.bool)
+    keep[5] = False
+    assert torch.allclose(Y[keep], X[keep], atol=1e-12) and Y[5] == 0
+    t = torch.from_numpy(rng.standard_normal((3, 4, 16)))
+    y = t.clone()
+    y[:, 2:4] *= 1.1                                              # signal channels 10 % off
+    assert torch.allclose(ff.signal_rel_err(y, t), torch.full((3,), 0.1, dtype=t.dtype), atol=1e-12)
+    assert torch.allclose(ff.sample_weights(t), 1.0 / t.pow(2).mean(dim=(1, 2)))
