@@ -210,15 +210,21 @@ int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cav
  * device.  This entry point has no counterpart in the reference.
  *
  * The caller passes the pulse's inputs and outputs (device pointers, as for
- * optifax_propagate; stats optional) and no handle.  The descriptor, twiddle
- * tables and cluster exchange buffer live in one static device array of about
- * 0.45 MB that each GPU loading the library reserves until the process exits.
- * n_points must be 8192 or 16384 (clusters of 2 or 4 CTAs of 4096 points);
- * other sizes, including anything above 16384, return OPTIFAX_ERR_UNSUPPORTED.
- * Variants BATCH_XTAL, BATCH_OP, NO_BC and HARD_BC are accepted.  The first call
- * on a device builds the twiddle tables in the array (set-up) and should come
- * before any stream capture.  Every call reuses the same array: calls that
- * overlap on the GPU race and must be serialised by the caller.
+ * optifax_propagate, validated by the same rules; stats optional) and no
+ * handle.  The descriptor, twiddle tables and cluster exchange buffer live in
+ * one static device array of 350,720 bytes (about 0.35 MB) that each GPU
+ * loading the library reserves until the process exits.  n_points must be 8192
+ * or 16384 (clusters of 2 or 4 CTAs of 4096 points); other sizes, including
+ * anything above 16384, return OPTIFAX_ERR_UNSUPPORTED.  Variants BATCH_XTAL,
+ * BATCH_OP, NO_BC and HARD_BC are accepted.
+ *
+ * Set-up: the first call in a CUDA context -- the first on a device, and again
+ * the first after that device's context has been replaced (cudaDeviceReset, or
+ * another context made current) -- finds the array's device address and builds
+ * the twiddle tables in it.  That call should come before any stream capture;
+ * made while its stream is capturing it returns OPTIFAX_ERR_UNSUPPORTED.  Every
+ * call reuses the same array and leaves its contents behind: calls that overlap
+ * on the GPU race and must be serialised by the caller.
  */
 int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t variant,
                               optifax_pulse_stats* stats, void* stream);

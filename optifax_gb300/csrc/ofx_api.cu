@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "ofx_kernels.cuh"
+#include "ofx_desc.cuh"
 #include "ofx_gnlse.cuh"
 #include "../../include/optifax.h"
 
@@ -101,6 +102,27 @@ int mark_done(optifax_context* h, cudaStream_t st) {
     return OPTIFAX_OK;
 }
 
+// Grow a handle-owned scratch buffer in stream order: the old buffer goes back
+// with cudaFreeAsync once the previous call's work is done (the stream waits on
+// done_ev first), the new one comes from cudaMallocAsync on the same stream, so
+// no other work on the device is waited for.
+int grow_scratch(optifax_context* h, void** buf, size_t* cap_bytes, size_t need_bytes, cudaStream_t st,
+                 const char* what) {
+    if (*buf && need_bytes <= *cap_bytes) return OPTIFAX_OK;
+    int rc = order_after_previous(h, st);
+    if (rc) return rc;
+    if (*buf) {
+        cudaError_t e = cudaFreeAsync(*buf, st);
+        if (e != cudaSuccess) return cuda_fail(h, e, what);
+        *buf = nullptr;
+        *cap_bytes = 0;
+    }
+    cudaError_t e = cudaMallocAsync(buf, need_bytes, st);
+    if (e != cudaSuccess) { *buf = nullptr; return cuda_fail(h, e, what); }
+    *cap_bytes = need_bytes;
+    return OPTIFAX_OK;
+}
+
 // W_n^e for e < count, built once per (n, count) map and kept for the context
 const Twiddle* get_table(optifax_context* h, std::map<int, Twiddle*>& cache, int n, int count,
                          cudaStream_t st, int* rc) {
@@ -135,14 +157,6 @@ const Twiddle* get_pass_twiddles(optifax_context* h, int M, cudaStream_t st, int
     return d;
 }
 
-uint64_t turns_fixed(long double radians) {
-    long double tw = radians / (2.0L * 3.14159265358979323846264338327950288L);
-    tw -= floorl(tw);                        // [0, 1)
-    long double x = tw * 18446744073709551616.0L;
-    if (x >= 18446744073709551615.0L) return 0;
-    return (uint64_t)x;
-}
-
 const std::vector<KernelEntry>& kernel_table() {
     static const std::vector<KernelEntry> tbl = [] {
         std::vector<KernelEntry> v;
@@ -159,33 +173,6 @@ const KernelEntry* find_kernel(int M, int C, int method) {
     for (const auto& k : kernel_table())
         if (k.M == M && k.C == C && k.method == method) return &k;
     return nullptr;
-}
-
-struct VariantCfg { int time_mode, abc_mode, guard, g_per_pulse, stepmods_rule, nee = 0; };
-
-bool variant_cfg(int variant, VariantCfg* v) {
-    switch (variant) {
-        case OPTIFAX_VARIANT_BATCH_XTAL: *v = {TIME_SHIFTED, ABC_SOFT, 1, 1, 128}; return true;
-        case OPTIFAX_VARIANT_BATCH_OP:   *v = {TIME_SHIFTED, ABC_SOFT, 1, 0, 128}; return true;
-        case OPTIFAX_VARIANT_NO_BC:      *v = {TIME_UNSHIFTED, ABC_NONE, 0, 0, 128}; return true;
-        case OPTIFAX_VARIANT_HARD_BC:    *v = {TIME_UNSHIFTED, ABC_HARD, 0, 0, 128}; return true;
-        case OPTIFAX_VARIANT_ODE23:      *v = {TIME_UNSHIFTED, ABC_SOFT, 0, 0, 256}; return true;
-        case OPTIFAX_VARIANT_NEE:        *v = {TIME_NEE, ABC_NEE, 0, 0, 128, 1}; return true;
-        default: return false;
-    }
-}
-
-int stepmods_limit_for(int N, int rule) {
-    // Dispersion_kernel records stepmods[k] in the thread with gx == k, gx in
-    // [0, gridDim.x * blockDim.x): ceil(N/128)*128 (BATCH kernels) or
-    // (N/256)*256 (ODE23, which launches N/256 blocks).
-    return rule == 128 ? ((N + 127) / 128) * 128 : (N / 256) * 256;
-}
-
-int n_chunks_for(int S, float sel, int guard) {
-    int nc = (int)((float)S / sel);
-    if (guard && (float)nc * sel < (float)S) nc += 1;
-    return nc;
 }
 
 int choose_M(int N, int cta_points) {
@@ -242,10 +229,11 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
             if (d.fb) need_xch += (size_t)g.M * g.C;    // OPO: the trip's crystal output (cavity scratch)
     }
     if (need_xch > h->xch_cap) {
-        if (h->d_xch) { cudaDeviceSynchronize(); cudaFree(h->d_xch); h->d_xch = nullptr; h->xch_cap = 0; }
-        cudaError_t e = cudaMalloc(&h->d_xch, need_xch * sizeof(float2));
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(exchange scratch)");
-        h->xch_cap = need_xch;
+        size_t cap = h->xch_cap * sizeof(float2);
+        int grc = grow_scratch(h, (void**)&h->d_xch, &cap, need_xch * sizeof(float2), st,
+                               "cudaMallocAsync(exchange scratch)");
+        h->xch_cap = cap / sizeof(float2);
+        if (grc) return grc;
     }
     std::vector<PulseDev> all;
     all.reserve(n_desc);
@@ -258,11 +246,9 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         }
     size_t nb = all.size() * sizeof(PulseDev);
     if (nb > h->desc_cap) {
-        if (h->d_desc) { cudaDeviceSynchronize(); cudaFree(h->d_desc); h->d_desc = nullptr; }
-        size_t cap = nb < 4096 ? 4096 : nb * 2;
-        cudaError_t e = cudaMalloc(&h->d_desc, cap);
-        if (e != cudaSuccess) { h->desc_cap = 0; return cuda_fail(h, e, "cudaMalloc(descriptors)"); }
-        h->desc_cap = cap;
+        int grc = grow_scratch(h, (void**)&h->d_desc, &h->desc_cap, nb < 4096 ? 4096 : nb * 2, st,
+                               "cudaMallocAsync(descriptors)");
+        if (grc) return grc;
     }
     int rc = order_after_previous(h, st);
     if (rc) return rc;
@@ -358,52 +344,11 @@ int launch_group(optifax_context* h, const std::vector<PulseDev>& descs, int M, 
     return launch_groups(h, groups, method, vc, shared, st);
 }
 
-bool is_pow2(long long x) { return x > 0 && (x & (x - 1)) == 0; }
-
 int fill_desc(optifax_context* h, const optifax_pulse& in, const VariantCfg& vc, PulseDev* d,
               optifax_pulse_stats* stats) {
-    if (!is_pow2(in.n_points) || in.n_points < 512 || in.n_points > 65536)
-        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_points must be a power of two in [512, 65536]");
-    if (in.n_steps < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_steps must be >= 1");
-    if (!(in.sel >= 1.0f)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "sel must be >= 1");
-    if (!(in.h > 0.0f) || !(in.dt > 0.0) || !(in.w0 > 0.0f))
-        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "h, dt and w0 must be positive");
-    if (!in.E_in || !in.A_out || !in.alpha || !in.beta || !in.G)
-        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "E_in, A_out, alpha, beta and G are required");
-    if ((in.trace && in.trace_cap < 0) || (in.forced && in.n_forced < 0))
-        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "negative trace/forced length");
-    const long long n_att_bound = 64LL * (in.n_steps + 16) + 64;
-    if (n_att_bound > 0x7fffffffLL || (long long)in.n_steps * 4 > (1LL << 24))
-        return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "n_steps too large (4*S must stay below 2^24)");
-    memset(d, 0, sizeof(*d));
-    d->E_in = (const float2*)in.E_in;
-    d->A_out = (float2*)in.A_out;
-    d->alpha = in.alpha;
-    d->beta = in.beta;
-    d->G = in.G;
-    d->Ap = (float2*)in.Ap;
-    d->stepmods = in.stepmods;
-    d->trace = in.trace;
-    d->forced = in.forced;
-    d->stats = stats;
-    d->bdiffw0 = in.bdiffw0;
-    d->dt = in.dt;
-    d->tau_theta = turns_fixed((long double)(double)in.w0 * (long double)in.dt);
-    d->tau_z4 = turns_fixed((long double)in.bdiffw0 * (long double)(double)in.h / 4.0L);
-    d->w0 = in.w0;
-    d->h = in.h;
-    d->max_err = in.max_err;
-    d->min_err = in.min_err;
-    d->sel = in.sel;
-    float invdt2 = (float)(1.0 / (2.0 * in.dt));
-    d->c_shock = invdt2 / in.w0;
-    d->N = in.n_points;
-    d->S = in.n_steps;
-    d->nchunks = n_chunks_for(in.n_steps, in.sel, vc.guard);
-    d->stepmods_limit = in.stepmods_limit > 0 ? in.stepmods_limit : stepmods_limit_for(in.n_points, vc.stepmods_rule);
-    d->trace_cap = in.trace ? in.trace_cap : 0;
-    d->n_forced = in.forced ? in.n_forced : 0;
-    return OPTIFAX_OK;
+    std::string why;
+    int rc = fill_pulse_desc(in, vc, d, stats, &why);
+    return rc ? fail(h, rc, why) : OPTIFAX_OK;
 }
 
 }  // namespace
@@ -650,17 +595,18 @@ extern "C" int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses
     if (!twp) return rc;
     const size_t need_k = (size_t)7 * M * n_pulses;
     if (need_k > h->gnlse_k_cap) {
-        if (h->d_gnlse_k) { cudaDeviceSynchronize(); cudaFree(h->d_gnlse_k); h->d_gnlse_k = nullptr; h->gnlse_k_cap = 0; }
-        cudaError_t e = cudaMalloc(&h->d_gnlse_k, need_k * sizeof(float2));
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(gnlse stage scratch)");
-        h->gnlse_k_cap = need_k;
+        size_t cap = h->gnlse_k_cap * sizeof(float2);
+        rc = grow_scratch(h, (void**)&h->d_gnlse_k, &cap, need_k * sizeof(float2), st,
+                          "cudaMallocAsync(gnlse stage scratch)");
+        h->gnlse_k_cap = cap / sizeof(float2);
+        if (rc) return rc;
     }
     if ((size_t)n_pulses > h->gnlse_desc_cap) {
-        if (h->d_gnlse_desc) { cudaDeviceSynchronize(); cudaFree(h->d_gnlse_desc); h->d_gnlse_desc = nullptr; }
-        h->gnlse_desc_cap = 0;
-        cudaError_t e = cudaMalloc(&h->d_gnlse_desc, sizeof(GnlseDev) * (size_t)n_pulses);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMalloc(gnlse descriptors)");
-        h->gnlse_desc_cap = (size_t)n_pulses;
+        size_t cap = h->gnlse_desc_cap * sizeof(GnlseDev);
+        rc = grow_scratch(h, (void**)&h->d_gnlse_desc, &cap, sizeof(GnlseDev) * (size_t)n_pulses, st,
+                          "cudaMallocAsync(gnlse descriptors)");
+        h->gnlse_desc_cap = cap / sizeof(GnlseDev);
+        if (rc) return rc;
     }
     for (int i = 0; i < n_pulses; ++i) d[(size_t)i].K = h->d_gnlse_k + (size_t)7 * M * i;
     rc = order_after_previous(h, st);

@@ -8,24 +8,33 @@
 // serves them.  The caller still passes every input and output; everything else
 // the pass needs -- the pulse descriptor, the FFT twiddle tables and the
 // cluster exchange buffer -- lives in one file-scope static device array of
-// fixed size (g_noalloc_scratch, about 0.45 MB), which every GPU that loads
-// this library reserves until the process exits.
+// fixed size (g_noalloc_scratch, 350,720 bytes, about 0.35 MB), which every GPU
+// that loads this library reserves until the process exits.
 //
 // The kernel is the clustered Heun crystal pass (4096 points per CTA, clusters
 // of 2 or 4 CTAs), so n_points must be 8192 or 16384; anything else, in
 // particular anything beyond 16384 points, is rejected with
-// OPTIFAX_ERR_UNSUPPORTED.  The first call on a device fills the twiddle
-// tables (set-up); make that first call before any stream capture.  All calls
-// share the array and it keeps the last call's contents; nothing in it has to
-// start at zero (each call rewrites the descriptor and every exchange value
-// before reading it).  Calls that overlap on the GPU (other streams, other host
-// threads) race on the array and must be serialised by the caller.
+// OPTIFAX_ERR_UNSUPPORTED.
+//
+// Set-up: the first call in a CUDA context (the first on a device, and the
+// first after that device's context was replaced, e.g. by cudaDeviceReset)
+// looks up the array's device address with cudaGetSymbolAddress and fills the
+// twiddle tables of both sizes.  That call must come before any stream capture;
+// made while its stream captures, it returns OPTIFAX_ERR_UNSUPPORTED and sets
+// nothing up.  Each call writes its descriptor with a one-thread kernel that
+// receives it as a kernel parameter (no host staging buffer), and every
+// exchange value is written before it is read, so nothing in the array has to
+// start at zero.  All calls share the array and it keeps the last call's
+// contents: calls that overlap on the GPU (other streams, other host threads)
+// race on it and must be serialised by the caller.
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "ofx_kernels.cuh"
+#include "ofx_desc.cuh"
 #include "../../include/optifax.h"
 
 using namespace ofx;
@@ -37,24 +46,53 @@ constexpr int kMaxN = 16384;             // cluster of 4
 constexpr size_t kDescBytes = 512;
 constexpr size_t kPassTw = kM + 16 * (kM / 256);          // pass-1 + pass-2 outer twiddles
 constexpr size_t kQuadTw = kM / 4;                         // W_M^y, y < M/4 (cluster exchange)
-constexpr size_t kLowTw = 64;                              // W_N^i, i < 64 (cluster exchange)
+constexpr size_t kLowTw = 64;                              // W_N^i, i < 64 (cluster exchange), per N
 constexpr size_t kXch = 2 * (size_t)kMaxN;                 // exchange buffer (complex)
 constexpr size_t kOffPass = kDescBytes;
 constexpr size_t kOffQuad = kOffPass + sizeof(Twiddle) * kPassTw;
-constexpr size_t kOffN = kOffQuad + sizeof(Twiddle) * kQuadTw;
-constexpr size_t kOffXch = kOffN + sizeof(Twiddle) * kLowTw;
+constexpr size_t kOffLow8k = kOffQuad + sizeof(Twiddle) * kQuadTw;     // W_8192^i
+constexpr size_t kOffLow16k = kOffLow8k + sizeof(Twiddle) * kLowTw;    // W_16384^i
+constexpr size_t kOffXch = kOffLow16k + sizeof(Twiddle) * kLowTw;
 constexpr size_t kBytes = kOffXch + sizeof(float2) * kXch;
 static_assert(sizeof(PulseDev) <= kDescBytes, "descriptor slot too small");
+static_assert(kBytes == 350720, "the documented size of the static array");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
+// Per device: the CUDA context the tables were built in and the array's device
+// address there.  A new context (a device reset, a context the caller created
+// and made current) reloads the module with a zeroed array, so set-up reruns.
 struct DeviceSetup {
-    unsigned char* base = nullptr;       // device address of g_noalloc_scratch
-    int n_table = 0;                     // N of the W_N table currently in the array
-    bool pass_tables = false;
+    unsigned char* base = nullptr;
+    unsigned long long ctx_id = 0;
+    bool ready = false;
 };
 std::mutex g_mutex;
 DeviceSetup g_setup[64];
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (the
+// library does not link the driver library itself)
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+bool current_context_id(unsigned long long* id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetIdFn)f;
+    });
+    void* ctx = nullptr;
+    return get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, id) == 0;
+}
 
 __global__ void noalloc_pass_twiddles(Twiddle* out, int L) {
     int lr = L / 16;
@@ -79,12 +117,19 @@ __global__ void noalloc_twiddles(Twiddle* out, int n, int count) {
     out[e] = Twiddle{cf, sf, (float)(1.0 / m2 - 1.0), 0.f};
 }
 
-uint64_t noalloc_turns(long double radians) {
-    long double tw = radians / (2.0L * 3.14159265358979323846264338327950288L);
-    tw -= floorl(tw);
-    long double x = tw * 18446744073709551616.0L;
-    if (x >= 18446744073709551615.0L) return 0;
-    return (uint64_t)x;
+// The call's descriptor arrives as a kernel parameter (copied at launch) and is
+// written into its slot of the array in stream order.
+__global__ void noalloc_put_desc(PulseDev* slot, PulseDev d) { *slot = d; }
+
+int setup_tables(unsigned char* base, cudaStream_t st) {
+    Twiddle* tw = reinterpret_cast<Twiddle*>(base + kOffPass);
+    noalloc_pass_twiddles<<<(kM + 255) / 256, 256, 0, st>>>(tw, kM);
+    noalloc_pass_twiddles<<<1, 256, 0, st>>>(tw + kM, kM / 16);
+    noalloc_twiddles<<<(int)((kQuadTw + 255) / 256), 256, 0, st>>>(
+        reinterpret_cast<Twiddle*>(base + kOffQuad), kM, (int)kQuadTw);
+    noalloc_twiddles<<<1, 64, 0, st>>>(reinterpret_cast<Twiddle*>(base + kOffLow8k), 8192, (int)kLowTw);
+    noalloc_twiddles<<<1, 64, 0, st>>>(reinterpret_cast<Twiddle*>(base + kOffLow16k), 16384, (int)kLowTw);
+    return cudaGetLastError() == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
 }
 
 }  // namespace
@@ -94,17 +139,13 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
     if (!pulse) return OPTIFAX_ERR_INVALID_ARGUMENT;
     const optifax_pulse& in = *pulse;
     if (in.n_points != 8192 && in.n_points != kMaxN) return OPTIFAX_ERR_UNSUPPORTED;
-    if (in.n_steps < 1 || !(in.sel >= 1.0f) || !(in.h > 0.0f) || !(in.dt > 0.0) || !(in.w0 > 0.0f) ||
-        !in.E_in || !in.A_out || !in.alpha || !in.beta || !in.G || (long long)in.n_steps * 4 > (1LL << 24))
+    if (variant != OPTIFAX_VARIANT_BATCH_XTAL && variant != OPTIFAX_VARIANT_BATCH_OP &&
+        variant != OPTIFAX_VARIANT_NO_BC && variant != OPTIFAX_VARIANT_HARD_BC)
         return OPTIFAX_ERR_INVALID_ARGUMENT;
-    int time_mode, abc_mode, guard, rule;
-    switch (variant) {
-        case OPTIFAX_VARIANT_BATCH_XTAL:
-        case OPTIFAX_VARIANT_BATCH_OP: time_mode = TIME_SHIFTED; abc_mode = ABC_SOFT; guard = 1; rule = 128; break;
-        case OPTIFAX_VARIANT_NO_BC: time_mode = TIME_UNSHIFTED; abc_mode = ABC_NONE; guard = 0; rule = 128; break;
-        case OPTIFAX_VARIANT_HARD_BC: time_mode = TIME_UNSHIFTED; abc_mode = ABC_HARD; guard = 0; rule = 128; break;
-        default: return OPTIFAX_ERR_INVALID_ARGUMENT;
-    }
+    VariantCfg vc;
+    if (!variant_cfg(variant, &vc)) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    PulseDev d;
+    if (fill_pulse_desc(in, vc, &d, stats, nullptr) != OPTIFAX_OK) return OPTIFAX_ERR_INVALID_ARGUMENT;
     const int N = in.n_points, C = N / kM;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return OPTIFAX_ERR_CUDA;
@@ -121,73 +162,39 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
         if (k.M == kM && k.C == C && k.method == OPTIFAX_HEUN) ke = &k;
     if (!ke) return OPTIFAX_ERR_UNSUPPORTED;
 
+    // the array's address in the current context (loads the module if needed)
     unsigned char* base = nullptr;
+    if (cudaGetSymbolAddress((void**)&base, g_noalloc_scratch) != cudaSuccess || !base) return OPTIFAX_ERR_CUDA;
+    unsigned long long ctx_id = 0;
+    if (!current_context_id(&ctx_id)) return OPTIFAX_ERR_CUDA;
     {
         std::lock_guard<std::mutex> lk(g_mutex);
         DeviceSetup& ds = g_setup[dev];
-        if (!ds.base) {
-            // set-up, once per device, with that device current
-            unsigned char* p = nullptr;
-            if (cudaGetSymbolAddress((void**)&p, g_noalloc_scratch) != cudaSuccess || !p) return OPTIFAX_ERR_CUDA;
-            ds.base = p;
-        }
-        base = ds.base;
-        if (!ds.pass_tables) {
-            Twiddle* tw = reinterpret_cast<Twiddle*>(base + kOffPass);
-            noalloc_pass_twiddles<<<(kM + 255) / 256, 256, 0, st>>>(tw, kM);
-            noalloc_pass_twiddles<<<1, 256, 0, st>>>(tw + kM, kM / 16);
-            noalloc_twiddles<<<(int)((kQuadTw + 255) / 256), 256, 0, st>>>(
-                reinterpret_cast<Twiddle*>(base + kOffQuad), kM, (int)kQuadTw);
-            if (cudaGetLastError() != cudaSuccess) return OPTIFAX_ERR_CUDA;
-            ds.pass_tables = true;
-        }
-        if (ds.n_table != N) {
-            noalloc_twiddles<<<1, 64, 0, st>>>(reinterpret_cast<Twiddle*>(base + kOffN), N, (int)kLowTw);
-            if (cudaGetLastError() != cudaSuccess) return OPTIFAX_ERR_CUDA;
-            ds.n_table = N;
+        if (!ds.ready || ds.ctx_id != ctx_id || ds.base != base) {
+            // set-up, once per context, with this device current; never under capture
+            cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+                return OPTIFAX_ERR_UNSUPPORTED;
+            ds.ready = false;
+            if (setup_tables(base, st) != OPTIFAX_OK) return OPTIFAX_ERR_CUDA;
+            ds.base = base;
+            ds.ctx_id = ctx_id;
+            ds.ready = true;
         }
     }
 
-    PulseDev d;
-    memset(&d, 0, sizeof(d));
-    d.E_in = (const float2*)in.E_in;
-    d.A_out = (float2*)in.A_out;
-    d.alpha = in.alpha;
-    d.beta = in.beta;
-    d.G = in.G;
-    d.Ap = (float2*)in.Ap;
-    d.stepmods = in.stepmods;
-    d.trace = in.trace;
-    d.forced = in.forced;
-    d.stats = stats;
-    d.bdiffw0 = in.bdiffw0;
-    d.dt = in.dt;
-    d.tau_theta = noalloc_turns((long double)(double)in.w0 * (long double)in.dt);
-    d.tau_z4 = noalloc_turns((long double)in.bdiffw0 * (long double)(double)in.h / 4.0L);
-    d.w0 = in.w0;
-    d.h = in.h;
-    d.max_err = in.max_err;
-    d.min_err = in.min_err;
-    d.sel = in.sel;
-    d.c_shock = (float)(1.0 / (2.0 * in.dt)) / in.w0;
-    d.N = N;
-    d.S = in.n_steps;
-    int nc = (int)((float)in.n_steps / in.sel);
-    if (guard && (float)nc * in.sel < (float)in.n_steps) nc += 1;
-    d.nchunks = nc;
-    d.stepmods_limit = in.stepmods_limit > 0 ? in.stepmods_limit : ((N + rule - 1) / rule) * rule;
-    d.trace_cap = in.trace ? in.trace_cap : 0;
-    d.n_forced = in.forced ? in.n_forced : 0;
     d.xch = reinterpret_cast<float2*>(base + kOffXch);
-    if (cudaMemcpyAsync(base, &d, sizeof(d), cudaMemcpyHostToDevice, st) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    PulseDev* slot = reinterpret_cast<PulseDev*>(base);
+    noalloc_put_desc<<<1, 1, 0, st>>>(slot, d);
+    if (cudaGetLastError() != cudaSuccess) return OPTIFAX_ERR_CUDA;
 
     if (cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ke->smem) != cudaSuccess)
         return OPTIFAX_ERR_CUDA;
     KernelCfg cfg;
     memset(&cfg, 0, sizeof(cfg));
-    cfg.time_mode = time_mode;
-    cfg.abc_mode = abc_mode;
-    cfg.guard = guard;
+    cfg.time_mode = vc.time_mode;
+    cfg.abc_mode = vc.abc_mode;
+    cfg.guard = vc.guard;
     cfg.shared_sched = 0;
     cfg.max_attempts_mul = 64;
     cfg.grid_flags = nullptr;
@@ -195,7 +202,7 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
     tabs.tw1 = reinterpret_cast<const Twiddle*>(base + kOffPass);
     tabs.tw2 = tabs.tw1 + kM;
     tabs.quad = reinterpret_cast<const Twiddle*>(base + kOffQuad);
-    tabs.low = reinterpret_cast<const Twiddle*>(base + kOffN);
+    tabs.low = reinterpret_cast<const Twiddle*>(base + (N == 8192 ? kOffLow8k : kOffLow16k));
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)C, 1, 1);
     lc.blockDim = dim3(kM / 16, 1, 1);
@@ -206,7 +213,6 @@ extern "C" int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t var
     attr.val.clusterDim.x = C; attr.val.clusterDim.y = 1; attr.val.clusterDim.z = 1;
     lc.attrs = &attr;
     lc.numAttrs = 1;
-    const PulseDev* dd = reinterpret_cast<const PulseDev*>(base);
-    if (cudaLaunchKernelEx(&lc, ke->fn, dd, tabs, cfg) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    if (cudaLaunchKernelEx(&lc, ke->fn, (const PulseDev*)slot, tabs, cfg) != cudaSuccess) return OPTIFAX_ERR_CUDA;
     return OPTIFAX_OK;
 }

@@ -29,9 +29,23 @@ _LIB_PATH = os.path.join(_HERE, "_build", "libref_mex.so")
 _lib = None
 
 
+def reference_kernel_sources():
+    """The reference's MEX source directory (toolbox/lib/MEXlib/src), or None where
+    the reference is absent (the GPU host: the cubins travel as built files).  The
+    checkout is found through OPTIFAX_REFERENCE, else at its location in the
+    build container."""
+    root = os.environ.get("OPTIFAX_REFERENCE", "/root/reference")
+    src = os.path.join(root, "toolbox", "lib", "MEXlib", "src")
+    return src if os.path.isdir(src) else None
+
+
 def build() -> None:
-    """Build the harness (and, where the reference source exists, the cubin)."""
-    subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    """Build the harness (and, where the reference source exists, the cubins)."""
+    cmd = ["make", "-s", "-C", _HERE, "ref"]
+    src = reference_kernel_sources()
+    if src:
+        cmd.append("REF_SRC=" + src)
+    subprocess.run(cmd, check=True)
 
 
 def available(cubin: str = CUBIN):

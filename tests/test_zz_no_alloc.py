@@ -9,9 +9,15 @@ device -- use optifax_propagate_noalloc, which keeps its working memory in a
 fixed static device array.  Two calls in a row must each reproduce the
 allocating entry point's output within the parity tolerance (1e-4 rel-L2),
 which also shows that the second call is not disturbed by what the first left
-in the shared array.  This file is collected last on purpose.
+in the shared array.  The set-up is tied to the CUDA context: a child process
+checks that a call made under stream capture before set-up is refused, and that
+a call after cudaDeviceReset (a new context, a zeroed array) still gives the
+same field.  This file is collected last on purpose.
 """
 import ctypes
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -20,6 +26,9 @@ import torch
 from tests._cases import make_case, rel_l2
 
 pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+VARIANTS = ["BATCH_XTAL", "BATCH_OP", "NO_BC", "HARD_BC"]
 
 
 def _pulse_struct(nat, E, out, al, be, G, si):
@@ -32,33 +41,130 @@ def _pulse_struct(nat, E, out, al, be, G, si):
     return d
 
 
-@pytest.mark.parametrize("N", [16384, 8192])
-def test_noalloc_matches_allocating_entry(N):
-    from optifax_gb300 import _native as nat
-    from optifax_gb300 import solver as sv
+def _inputs(N):
     win, si, E = make_case(N=N, length=0.1e-3, power=2.0)
     dev = torch.device("cuda:0")
-    Et = torch.from_numpy(E[0].astype(np.complex64)).to(dev)
-    al = torch.from_numpy(si.alpha).to(dev)
-    be = torch.from_numpy(si.beta).to(dev)
-    G = torch.from_numpy(si.G).to(dev)
+    t = lambda a: torch.from_numpy(a).to(dev)
+    return si, t(E[0].astype(np.complex64)), t(si.alpha), t(si.beta), t(si.G)
+
+
+def _allocating(nat, sv, si, Et, al, be, G, variant):
     spec = sv.PulseSpec(E=Et, alpha=al, beta=be, G=G, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, dt=si.dt,
                         max_err=si.max_err, min_err=si.min_err, sel=si.sel, n_steps=si.n_steps)
-    outs, _ = sv.propagate([spec], method=nat.HEUN, variant=nat.VARIANT_BATCH_XTAL, cta_points=4096)
+    outs, _ = sv.propagate([spec], method=nat.HEUN, variant=variant, cta_points=4096)
     torch.cuda.synchronize()
-    ref = outs[0].cpu().numpy()
+    return outs[0].cpu().numpy()
+
+
+def _noalloc(nat, sv, si, Et, al, be, G, variant):
     lib = nat.load()
     stream = torch.cuda.current_stream().cuda_stream
+    out = torch.zeros_like(Et)
+    stats = torch.zeros((1, nat.STATS_BYTES // 4), dtype=torch.int32, device=Et.device)
+    d = _pulse_struct(nat, Et, out, al, be, G, si)
+    rc = lib.optifax_propagate_noalloc(ctypes.byref(d), variant, stats.data_ptr(), stream)
+    assert rc == 0, rc
+    torch.cuda.synchronize()
+    st = sv.decode_stats(stats)[0]
+    assert st["status"] == 0 and st["attempts"] > 0
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("N", [16384, 8192])
+def test_noalloc_matches_allocating_entry(N, variant):
+    from optifax_gb300 import _native as nat
+    from optifax_gb300 import solver as sv
+    v = getattr(nat, "VARIANT_" + variant)
+    si, Et, al, be, G = _inputs(N)
+    ref = _allocating(nat, sv, si, Et, al, be, G, v)
     for call in range(2):
-        out = torch.zeros_like(Et)
-        stats = torch.zeros((1, nat.STATS_BYTES // 4), dtype=torch.int32, device=dev)
-        d = _pulse_struct(nat, Et, out, al, be, G, si)
-        rc = lib.optifax_propagate_noalloc(ctypes.byref(d), nat.VARIANT_BATCH_XTAL, stats.data_ptr(), stream)
-        assert rc == 0, rc
-        torch.cuda.synchronize()
-        st = sv.decode_stats(stats)[0]
-        assert st["status"] == 0 and st["attempts"] > 0
-        assert rel_l2(out.cpu().numpy(), ref) <= 1e-4, (call, rel_l2(out.cpu().numpy(), ref))
+        out = _noalloc(nat, sv, si, Et, al, be, G, v)
+        assert rel_l2(out, ref) <= 1e-4, (call, rel_l2(out, ref))
+
+
+def test_noalloc_alternating_sizes_on_one_stream():
+    """8192, 16384, 8192 points in a row: each size's tables stay valid."""
+    from optifax_gb300 import _native as nat
+    from optifax_gb300 import solver as sv
+    v = nat.VARIANT_BATCH_XTAL
+    cases = {N: _inputs(N) for N in (8192, 16384)}
+    refs = {N: _allocating(nat, sv, *cases[N], v) for N in cases}
+    for N in (8192, 16384, 8192):
+        out = _noalloc(nat, sv, *cases[N], v)
+        assert rel_l2(out, refs[N]) <= 1e-4, (N, rel_l2(out, refs[N]))
+
+
+_CHILD = r"""
+import ctypes, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from optifax_gb300 import _native as nat
+from tests._cases import make_case
+lib = nat.load()
+rt = ctypes.CDLL("libcudart.so.13")
+rt.cudaGetErrorString.restype = ctypes.c_char_p
+
+def ok(rc, what):
+    if rc != 0:
+        raise SystemExit(f"{what}: {rt.cudaGetErrorString(rc).decode()}")
+
+win, si, E = make_case(N=8192, length=0.1e-3, power=2.0)
+host = {"E": E[0].astype(np.complex64), "alpha": si.alpha, "beta": si.beta, "G": si.G}
+
+def device_inputs():
+    bufs = {}
+    for k, a in host.items():
+        p = ctypes.c_void_p()
+        ok(rt.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(a.nbytes)), "cudaMalloc")
+        ok(rt.cudaMemcpy(p, a.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(a.nbytes), 1), "cudaMemcpy H2D")
+        bufs[k] = p
+    out = ctypes.c_void_p()
+    ok(rt.cudaMalloc(ctypes.byref(out), ctypes.c_size_t(host["E"].nbytes)), "cudaMalloc")
+    return bufs, out
+
+def call(bufs, out, stream):
+    d = nat.OptifaxPulse()
+    d.n_points, d.n_steps = 8192, si.n_steps
+    d.E_in, d.A_out = bufs["E"].value, out.value
+    d.alpha, d.beta, d.G = bufs["alpha"].value, bufs["beta"].value, bufs["G"].value
+    d.w0, d.h, d.bdiffw0, d.dt = si.w0, si.h, si.bdiffw0, si.dt
+    d.max_err, d.min_err, d.sel = si.max_err, si.min_err, si.sel
+    return lib.optifax_propagate_noalloc(ctypes.byref(d), nat.VARIANT_BATCH_XTAL, None, stream)
+
+def result(out):
+    h = np.empty_like(host["E"])
+    ok(rt.cudaDeviceSynchronize(), "sync")
+    ok(rt.cudaMemcpy(h.ctypes.data_as(ctypes.c_void_p), out, ctypes.c_size_t(h.nbytes), 2), "cudaMemcpy D2H")
+    return h
+
+bufs, out = device_inputs()
+# the first call of the context under stream capture is refused before any set-up
+s = ctypes.c_void_p()
+ok(rt.cudaStreamCreateWithFlags(ctypes.byref(s), 1), "cudaStreamCreate")
+ok(rt.cudaStreamBeginCapture(s, 2), "cudaStreamBeginCapture")    # relaxed mode
+rc_cap = call(bufs, out, s)
+g = ctypes.c_void_p()
+ok(rt.cudaStreamEndCapture(s, ctypes.byref(g)), "cudaStreamEndCapture")
+if g.value:
+    rt.cudaGraphDestroy(g)
+assert rc_cap == 2, f"call under capture before set-up returned {rc_cap}"
+assert call(bufs, out, None) == 0
+first = result(out)
+assert np.all(np.isfinite(first)) and np.abs(first).max() > 0
+# a new context: the array is reloaded zeroed; the next call must set up again
+ok(rt.cudaDeviceReset(), "cudaDeviceReset")
+bufs, out = device_inputs()
+assert call(bufs, out, None) == 0
+second = result(out)
+assert np.array_equal(first, second), float(np.abs(first - second).max())
+print("reset-ok")
+"""
+
+
+def test_noalloc_setup_follows_the_context():
+    r = subprocess.run([sys.executable, "-c", _CHILD, ROOT], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and "reset-ok" in r.stdout, r.stdout + r.stderr
 
 
 def test_noalloc_rejects_sizes_beyond_maximum():
