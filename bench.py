@@ -98,10 +98,31 @@ def _peaks():
 
 
 def host_cores() -> int:
+    """CPUs this process may use: its affinity mask, capped by a cgroup CPU quota
+    (a container can see every core of the host but be granted fewer)."""
     try:
-        return len(os.sched_getaffinity(0))
+        n = len(os.sched_getaffinity(0))
     except AttributeError:
-        return os.cpu_count() or 1
+        n = os.cpu_count() or 1
+    quota = None
+    try:
+        with open("/sys/fs/cgroup/cpu.max") as f:               # cgroup v2: "<quota> <period>" or "max <period>"
+            q, per = f.read().split()[:2]
+            if q != "max":
+                quota = int(q) / int(per)
+    except (OSError, ValueError):
+        try:
+            with open("/sys/fs/cgroup/cpu/cpu.cfs_quota_us") as f:   # cgroup v1
+                q = int(f.read())
+            with open("/sys/fs/cgroup/cpu/cpu.cfs_period_us") as f:
+                per = int(f.read())
+            if q > 0:
+                quota = q / per
+        except (OSError, ValueError):
+            pass
+    if quota is not None:
+        n = max(1, min(n, int(quota)))
+    return n
 
 
 def oracle_threads(spec, field=None, fraction=0.004):
@@ -203,12 +224,39 @@ def cpu_sweep_sample(insts, gpu_stats, cores, n_sample=16, fraction=0.02):
                       f"sweep by attempts x N log2 N with the GPU's attempt counts"}
 
 
-def reference_gpu_sample(spec, fraction=0.1):
+def reference_buildup(spec, trips=5):
+    """A built-up cavity field for the reference arm, made by the reference's own
+    code: `trips` round trips with its CUDA kernels (OPO_CUDA_BATCH_XTAL.cu, driven
+    as its MEX driver does) and the cavity transfer of OpticalSim.m:230-288 on the
+    host.  Returns (crystal input of the next trip, description); without the
+    compiled kernels, the first trip's input."""
+    import numpy as np
+    from oracle import ref_mex
+    from optifax_gb300.opo import build_cavity
+    arr = build_cavity(spec)
+    ok, why = ref_mex.available()
+    if not ok:
+        return arr.E0, f"the first trip's crystal input ({why})"
+    si = arr.si
+    E = arr.E0
+    try:
+        for _ in range(trips):
+            r = ref_mex.run(E, si.alpha, si.G, si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps,
+                            dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=si.sel, trace_cap=0)
+            X = np.fft.fft(r.A[0].astype(np.complex128))
+            E = np.fft.ifft(X * arr.feedback + arr.pump)
+    except OSError as exc:     # no GPU driver on this host
+        return arr.E0, f"the first trip's crystal input (reference kernels not runnable: {exc})"
+    return E, (f"the crystal input after {trips} round trips run by the reference's own CUDA kernels "
+               f"(a built-up cavity)")
+
+
+def reference_gpu_sample(spec, fraction=0.1, field=None, start="the first trip's input"):
     """The reference's own CUDA kernels (OPO_CUDA_BATCH_XTAL.cu compiled unmodified,
     driven with cuFFT as its MEX driver does) on the first `fraction` of one crystal
-    pass from the first trip's input; the time per attempt, scaled to a built-up
-    round trip (0.97 attempts per z-sample), bounds the reference's round trips/s
-    from above (its cavity step runs on the host in MATLAB and is not counted)."""
+    pass from the first trip's input; the time per z-sample of that sample, scaled
+    to the whole pass, bounds the reference's round trips/s from above (its cavity
+    step runs on the host in MATLAB and is not counted)."""
     import numpy as np
     from oracle import ref_mex
     from optifax_gb300.opo import build_cavity
@@ -219,54 +267,116 @@ def reference_gpu_sample(spec, fraction=0.1):
     si = arr.si
     S = max(8, int(si.n_steps * fraction))
     sel = float(np.ceil(S / 4))
-    ref_mex.run(arr.E0, si.alpha, si.G[:S // 10], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+    E = arr.E0 if field is None else field
+    ref_mex.run(E, si.alpha, si.G[:S // 10], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
                 n_steps=S // 10, dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=sel / 10,
                 trace_cap=0)                       # warm-up: module load, cuFFT plan
-    r = ref_mex.run(arr.E0, si.alpha, si.G[:S], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+    r = ref_mex.run(E, si.alpha, si.G[:S], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
                     n_steps=S, dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=sel, trace_cap=0)
     per_attempt = r.seconds / r.attempts
-    per_trip = per_attempt * 0.97 * si.n_steps
+    per_trip = per_attempt * (r.attempts / S) * si.n_steps     # the sample's own attempts per z-sample
     return {"value": 1.0 / per_trip, "unit": UNIT, "us_per_attempt": per_attempt * 1e6,
             "kind": "reference CUDA kernels (cubin of OPO_CUDA_BATCH_XTAL.cu) + cuFFT, host-driven "
                     "as OPO_TEST_CUDA: 2 device syncs and a flag read-back per attempt",
-            "sample": f"first {S} of {si.n_steps} steps of one 5 mm pass from the first trip's input "
-                      f"({r.attempts} attempts, {r.seconds:.2f} s), scaled by attempts to a built-up "
-                      f"round trip; crystal pass only (upper bound on round trips/s)"}
+            "sample": f"first {S} of {si.n_steps} steps of one 5 mm pass from {start} "
+                      f"({r.attempts} attempts, {r.seconds:.2f} s), scaled by z-samples to the whole pass; "
+                      f"crystal pass only (upper bound on round trips/s)"}
+
+
+def accuracy_record(spec, E_in, fp64, device=0):
+    """FP32 propagator against the plain FP64 solver on the bench's own workload:
+    one 5 mm crystal pass of the 2^14-point cavity from the same crystal input (the
+    timed window's, a built-up cavity field).  Field rel-L2 over the whole spectrum
+    and over the fed-back band, the relative error of each energy tally (output,
+    output signal, intracavity, pump band), and whether the two step schedules
+    are identical attempt for attempt."""
+    import numpy as np
+    import torch
+    from optifax_gb300 import solver as sv, _native as nat
+    from optifax_gb300.opo import build_cavity
+    arr = build_cavity(spec)
+    si = arr.si
+    dev = torch.device(f"cuda:{device}")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    cap = 4 * si.n_steps
+    p = sv.PulseSpec(E=t(np.asarray(E_in).astype(np.complex64)), alpha=t(si.alpha), beta=t(si.beta), G=t(si.G),
+                     w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, dt=si.dt, max_err=si.max_err, min_err=si.min_err,
+                     sel=si.sel, n_steps=si.n_steps, trace_cap=cap)
+    outs, stats = sv.propagate([p], method=nat.HEUN, variant=nat.VARIANT_BATCH_XTAL)
+    torch.cuda.synchronize(dev)
+    st = sv.decode_stats(stats)[0]
+    X32 = np.fft.fft(outs[0].cpu().numpy().astype(np.complex128))
+    X64 = np.fft.fft(fp64["first_pass_out"])
+    band = np.abs(arr.feedback) > 0
+    rel = lambda a, b: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    names = ["output", "output_signal", "intracavity", "pump_band"]
+    e32, e64 = arr.tally_w @ np.abs(X32) ** 2, arr.tally_w @ np.abs(X64) ** 2
+    tr32 = p.trace.cpu().numpy()[:min(st["attempts"], cap)]
+    tr64 = fp64["first_pass_trace"]
+    key = lambda tr: np.stack([tr[:, 0], tr[:, 1], (tr[:, 2] >> 3) & 1], axis=1)
+    same = tr64 is not None and tr32.shape == tr64.shape and bool(np.array_equal(key(tr32), key(tr64)))
+    first_fork = None
+    if not same and tr64 is not None:
+        n = min(len(tr32), len(tr64))
+        d = np.nonzero(np.any(key(tr32[:n]) != key(tr64[:n]), axis=1))[0]
+        first_fork = int(d[0]) if len(d) else n
+    return {"what": "one 5 mm crystal pass, FP32 propagator vs plain FP64 solver, same built-up crystal input",
+            "field_rel_l2": rel(X32, X64), "fed_back_band_rel_l2": rel(X32[band], X64[band]),
+            "energy_rel_err": {n_: float(abs(a - b) / max(abs(b), 1e-300)) for n_, a, b in zip(names, e32, e64)},
+            "schedule_identical": same, "first_fork_attempt": first_fork,
+            "attempts_fp32": int(st["attempts"]), "attempts_fp64": int(len(tr64)) if tr64 is not None else None}
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU path restated in C (FP64 oracle);
-    the reference's own CPU code is MATLAB (NEE_CPU.m) and cannot run here.
-    The line also carries the reference's own CUDA kernels timed on this GPU
-    (``reference_gpu``), where their cubin is present."""
+    """--impl reference: the reference's CPU path restated in C (FP64 oracle); the
+    reference's own CPU code is MATLAB (NEE_CPU.m) and cannot run here.
+
+    A step is one segment of the 5 mm crystal pass: 1/50 of its z-samples (the
+    first trip's crystal input, each step over the next segment's QPM signs).  The
+    value is the round trips per second this rate amounts to: segments completed
+    / 50 per second of measured time, so ms_per_step x steps is the time actually
+    spent.  Threads: the faster of one and every host thread by a calibration
+    sample.  The line also carries the reference's own CUDA kernels timed on this
+    GPU (``reference_gpu``) where their cubin is present."""
+    import numpy as np
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    spec = _spec()
-    vals = []
+    from oracle import oracle as orc
     from optifax_gb300.opo import build_cavity
-    s_total = build_cavity(spec).si.n_steps
-    threads, times = oracle_threads(spec)
+    spec = _spec()
+    arr = build_cavity(spec)
+    si = arr.si
+    S = si.n_steps
+    seg = S // 50
+    E_start, start = reference_buildup(spec, trips=5)
+    threads, cal = oracle_threads(spec, field=E_start)
+    times, attempts = [], 0
     for i in range(args.warmup + args.steps):
-        # the built-up cavity runs at stepmod ~ 1 (about one attempt per z-sample)
-        r = cpu_oracle_sample(spec, fraction=0.02, threads=threads, attempts_per_trip=0.97 * s_total)
+        g0 = (i * seg) % (S - seg + 1)
+        t0 = time.perf_counter()
+        r = orc.run(E_start, si.alpha, si.G[g0:g0 + seg], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                    n_steps=seg, dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=float(np.ceil(seg / 4)),
+                    nthreads=threads)
+        el = time.perf_counter() - t0
         if i >= args.warmup:
-            vals.append(r["value"])
-    v = statistics.mean(vals)
+            times.append(el)
+            attempts += r.stats[0]["attempts"]
+    total = sum(times)
+    v = (len(times) * seg / S) / total
+    sample = (f"each step: FP64 C oracle over {seg} of the {S} z-samples of one 5 mm pass (1/50 of a round trip's "
+              f"crystal pass; the cavity transfer is not counted) from {start}, "
+              f"{attempts} attempts in {total:.1f} s over {len(times)} steps, on {threads} thread"
+              f"{'s' if threads > 1 else ''} (calibration: " + ", ".join(f"{k}: {t_:.2f} s" for k, t_ in sorted(cal.items()))
+              + f"; {host_cores()} host threads); the reference CPU path NEE_CPU.m is MATLAB")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "each step: FP64 C oracle over the first 2% of one 5 mm pass, scaled "
-                                       "by attempts to a built-up round trip (0.97 attempts per z-sample, as "
-                                       "measured on the GPU), on the faster of 1 thread and all "
-                                       f"{host_cores()} host threads by a calibration sample ("
-                                       + ", ".join(f"{k}: {t:.2f} s" for k, t in sorted(times.items()))
-                                       + "); the reference CPU path NEE_CPU.m is MATLAB"},
+            "data": "synthetic", "config": {"workload": WORKLOAD, "step": "1/50 of one round trip's crystal pass"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     try:
-        line["reference_gpu"] = reference_gpu_sample(spec)
+        line["reference_gpu"] = reference_gpu_sample(spec, field=E_start, start=start)
     except Exception as exc:  # noqa: BLE001
         line["reference_gpu"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     print(json.dumps(line))
@@ -415,17 +525,18 @@ def run_gnlse(args):
     print(json.dumps(line))
 
 
-def run_sweep(args):
+def sweep_record(steps, warmup, sweep_size=256, cpu_baseline=True, cpu_kw=None):
     """Config 3: a batch of crystal passes with uneven grids (2^12..2^16), crystals
     (0.5-10 mm, 28-32 um), pumps (0.5-3 W, 100-300 fs), seed 2, in one call.
-    A step is one whole batch; value = instances per second."""
+    A step is one whole batch; value = instances per second.  Sharded over the
+    ranks of an initialised process group (contiguous instance ranges balanced by
+    N log2(N) S); rank 0 returns the line, the others None."""
     import numpy as np
     import torch
     from optifax_gb300 import sweep, solver as sv, dist, physics as ph
     rank, world, local = dist.init("nccl")
     torch.cuda.set_device(local)
-    all_insts = sweep.uneven_sweep_instances(n=args.sweep_size, seed=2)
-    # independent passes: contiguous instance ranges balanced by N log2(N) S per rank
+    all_insts = sweep.uneven_sweep_instances(n=sweep_size, seed=2)
     costs = [dist.pass_cost(i.n_points, ph.Crystal(i.length, i.period).n_steps) for i in all_insts]
     part = dist.partition_by_cost(costs, world)[rank]
     insts = [all_insts[i] for i in part]
@@ -441,12 +552,14 @@ def run_sweep(args):
     prep_dev_s = time.perf_counter() - t0
     tuned = sv.autotune(sorted({i.n_points for i in insts}), device=local)
     stream = torch.cuda.current_stream()
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, warmup)):
         sv.propagate(specs, stream=stream)
     torch.cuda.synchronize()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")   # 256 MB > L2
     times, atts = [], []
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
+            flush.fill_(1.0)
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             dist.barrier()
             torch.cuda.synchronize()
@@ -463,28 +576,36 @@ def run_sweep(args):
     local_att = int(sum(s_["attempts"] for s_ in stats))
     gathered = dist.gather_to_rank0({"point_attempts": local_pa, "attempts": local_att, "n": len(insts)})
     if rank != 0:
-        return
+        return None
     point_attempts = sum(g["point_attempts"] for g in gathered)
     attempts = sum(g["attempts"] for g in gathered)
     peak, peak_kind = _peaks()
     achieved = 16.0 * point_attempts / t / 1e9
     line = {"metric": "batched crystal passes/s (uneven sweep)", "value": len(all_insts) / t, "unit": "passes/s",
-            "n_gpus": world, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": t * 1000.0,
+            "n_gpus": world, "steps": steps, "warmup": max(1, warmup), "ms_per_step": t * 1000.0,
             "higher_is_better": True,
             "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"uneven sweep: {len(all_insts)} instances, N 2^12..2^16, L 0.5-10 mm, "
                                    "period 28-32 um, 0.5-3 W, 100-300 fs, seed 2", "autotuned_cta_points": tuned,
                        "parallelism": f"{world} rank(s), contiguous instance ranges balanced by N log2(N) S",
                        "host_prep_s": prep_s, "device_prep_s": prep_dev_s, "point_attempts": point_attempts,
-                       "attempts": attempts},
+                       "attempts": attempts,
+                       "l2": "flushed (256 MB write) before every timed call"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                         "algorithmic": "16 B per grid point per step attempt"},
+                         "algorithmic": "16 B per grid point per step attempt (sum over instances of "
+                                        "16 N attempts) / event-timed call"},
             "gpu_launches": len({(i.n_points) for i in insts}),
             "clocks": clk.summary()}
-    if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_sweep_sample(insts, stats, os.cpu_count() or 1)
-    print(json.dumps(line))
+    if world == 1 and cpu_baseline:
+        line["cpu_baseline"] = cpu_sweep_sample(insts, stats, host_cores(), **(cpu_kw or {}))
+    return line
+
+
+def run_sweep(args):
+    line = sweep_record(args.steps, args.warmup, args.sweep_size, not args.no_cpu_baseline)
+    if line is not None:
+        print(json.dumps(line))
 
 
 def main():
@@ -499,8 +620,11 @@ def main():
                     help="opo: 2^14-point SPOPO round trips (default line); sweep: 256 uneven batched passes; "
                          "gnlse: chi(3) fibre power scan (152 pulses)")
     ap.add_argument("--sweep-size", type=int, default=256)
-    ap.add_argument("--fp64-trips", type=int, default=1,
-                    help="round trips of the plain FP64 solver timed beside the line (0: skip)")
+    ap.add_argument("--fp64-trips", type=int, default=2,
+                    help="round trips of the plain FP64 solver timed beside the line, from the timed window's "
+                         "crystal input (0: skip; also the accuracy record's FP64 side)")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="leave out the uneven-sweep sub-record of the default line")
     ap.add_argument("--fno-case", type=int, default=0,
                     help="profiling case: surrogate training steps at this batch size, no JSON bench line")
     ap.add_argument("--pass-case", default=None,
@@ -599,14 +723,29 @@ def main():
                                 attempts_per_trip=attempts / K)
 
     # the plain full-FP64 GPU solver (optifax_propagate_fp64, host cavity transfer in
-    # FP64) on the same crystal input as the timed window: the metric's comparator
-    fp64 = None
+    # FP64) on the same crystal input as the timed window: the metric's comparator,
+    # and the FP64 side of the accuracy record
+    fp64 = accuracy = None
     if rank == 0 and args.fp64_trips > 0:
         from optifax_gb300 import fastforward as ff
-        r64 = ff.fp64_plain_trips(spec, args.fp64_trips, device=local, E0=timed_input)
+        S = sim.arrays.si.n_steps
+        r64 = ff.fp64_plain_trips(spec, args.fp64_trips, device=local, E0=timed_input, trace_cap=4 * S)
         fp64 = {"trips_per_s": r64["trips_per_s"], "s_per_trip": r64["s_per_trip"], "trips": r64["trips"],
                 "attempts": r64["attempts"], "speedup_of_value": value / r64["trips_per_s"],
-                "note": "wall clock, one kernel per sub-operation and a host flag read-back per attempt"}
+                "note": "CUDA events around all trips; one kernel per sub-operation and a host flag "
+                        "read-back per attempt"}
+        accuracy = accuracy_record(spec, timed_input, r64, device=local)
+        # the same trips through the FP32 OPO kernel from the same input: next crystal input after each
+        sim.field = torch.from_numpy(timed_input.astype(np.complex64)).to(dev)
+        r32 = sim.run(args.fp64_trips, stream=stream)
+        e32 = r32.field.cpu().numpy().astype(np.complex128)
+        accuracy["after_trips"] = args.fp64_trips
+        accuracy["next_input_rel_l2_after_trips"] = float(np.linalg.norm(e32 - r64["field"]) /
+                                                          np.linalg.norm(r64["field"]))
+
+    sweep_line = None
+    if rank == 0 and world == 1 and not args.no_sweep:
+        sweep_line = sweep_record(1, 1, cpu_kw={"n_sample": 8, "fraction": 0.01})
 
     M = args.cta_points or min(N, 4096)
     if rank == 0:
@@ -636,6 +775,8 @@ def main():
             "gpu_launches": 1,
             "clocks": clk.summary(),
             "fp64_plain": fp64,
+            "accuracy": accuracy,
+            "sweep": sweep_line,
         }
         print(json.dumps(line))
     if world > 1:

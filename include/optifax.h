@@ -233,18 +233,20 @@ int optifax_propagate_noalloc(const optifax_pulse* pulse, int32_t variant,
  * The plain full-FP64 crystal pass (Heun schedule of OPO_CUDA_BATCH_XTAL.cu:373-525
  * and its BATCH_OP / NO_BC / HARD_BC variants, computed in double precision
  * throughout, as the reference's FP64 MATLAB solver NEE_CPU.m computes it on the
- * CPU).  It is the FP64 comparator of the FP32 propagator: one kernel per
- * sub-operation over global memory and a host-side step decision after a flag
- * read-back every attempt, like the reference's MEX driver.  The reference has no
- * FP64 GPU entry point; this one takes the MEX argument list with double arrays.
+ * CPU).  It is the FP64 comparator of the FP32 propagator: the same persistent
+ * design (one launch per pass, the field on chip in a thread-block cluster of up
+ * to 16 CTAs) with every value in double.  The reference has no FP64 GPU entry
+ * point; this one takes the MEX argument list with double arrays.
  *
  * E_in, A_out: DEVICE arrays of n_pulses x n_points complex doubles (interleaved);
  * alpha, beta: DEVICE, n_points doubles; G: DEVICE, n_steps doubles, or
  * n_pulses x n_steps when g_per_pulse.  All pulses share one step schedule (the
- * reference's batch rule).  trace_host (optional, HOST, 3 x trace_cap int32):
- * per attempt {k, stepmod, flags | 8 if accepted}; stats_host (optional, HOST).
- * Variant ODE23 is not offered; NEE follows NEE_CPU.m (the snapshot outputs are not
- * produced by this entry).  Calls on one device are serialised internally.
+ * reference's batch rule; n_pulses x clusters must fit one wave of SMs).
+ * trace_host (optional, HOST, 3 x trace_cap int32): per attempt {k, stepmod,
+ * flags | 8 if accepted}; stats_host (optional, HOST).  Variant ODE23 is not
+ * offered; NEE follows NEE_CPU.m for grids up to 2^14 points (the snapshot
+ * outputs are not produced by this entry).  Calls on one device are serialised
+ * internally, and each call waits for its stream before returning.
  */
 int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_t n_steps,
                            const double* E_in, double* A_out, const double* alpha,
@@ -253,6 +255,24 @@ int optifax_propagate_fp64(int32_t n_points, int32_t n_pulses, int32_t n_steps,
                            double max_err, double min_err, double sel, int32_t variant,
                            int32_t* trace_host, int32_t trace_cap,
                            optifax_pulse_stats* stats_host, void* stream);
+
+/*
+ * The float-float crystal pass: the same schedule, arguments and results as
+ * optifax_propagate_fp64, with the field, the stage sums, the nonlinear drive
+ * and every transform held as unevaluated sums of two FP32 values (~48-bit
+ * significands) and the step decisions taken at FP64 precision.  For passes
+ * whose parametric gain amplifies the FP32 field's rounding beyond the
+ * tolerance (a long chirped crystal), at a fraction of the FP64 kernel's time:
+ * GB300 runs FP32 about 64 times faster than FP64.  No counterpart in the
+ * reference.  Variants BATCH_XTAL, BATCH_OP, NO_BC, HARD_BC.
+ */
+int optifax_propagate_f32x2(int32_t n_points, int32_t n_pulses, int32_t n_steps,
+                            const double* E_in, double* A_out, const double* alpha,
+                            const double* beta, const double* G, int32_t g_per_pulse,
+                            double w0, double bdiffw0, double step_h, double dt,
+                            double max_err, double min_err, double sel, int32_t variant,
+                            int32_t* trace_host, int32_t trace_cap,
+                            optifax_pulse_stats* stats_host, void* stream);
 
 /*
  * Surrogate-network building block: C[M, N] (+)= A[M, K] . B[N, K]^T on the tensor

@@ -16,7 +16,7 @@ PULSE_NAN, PULSE_ATTEMPT_LIMIT = 0x1, 0x2
 
 EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifax_last_error",
            "optifax_opo_mex_batch", "optifax_propagate", "optifax_opo_run", "optifax_propagate_noalloc",
-           "optifax_propagate_fp64", "optifax_gemm_bf16", "optifax_tc_error",
+           "optifax_propagate_fp64", "optifax_propagate_f32x2", "optifax_gemm_bf16", "optifax_tc_error",
            "optifax_fno_param_count", "optifax_fno_create", "optifax_fno_destroy", "optifax_fno_set_params",
            "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
            "optifax_ff_encode", "optifax_ff_step",
@@ -84,6 +84,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_propagate_fp64.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, i32, f64, f64, f64, f64,
                                            f64, f64, f64, i32, vp, i32, vp, vp]
     lib.optifax_propagate_fp64.restype = ctypes.c_int
+    lib.optifax_propagate_f32x2.argtypes = lib.optifax_propagate_fp64.argtypes
+    lib.optifax_propagate_f32x2.restype = ctypes.c_int
     i64 = ctypes.c_int64
     lib.optifax_gemm_bf16.argtypes = [vp, i64, i64, vp, i64, i64, vp, i64, i32, i32, i32, i32, i32, vp]
     lib.optifax_gemm_bf16.restype = ctypes.c_int

@@ -15,10 +15,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "liboptifax.so")
-SOURCES = ["ofx_api.cu", "ofx_k_heun_large.cu", "ofx_k_heun_small.cu", "ofx_k_rk23.cu", "ofx_k_heun_nee.cu", "ofx_noalloc.cu", "ofx_fp64.cu", "ofx_gemm.cu", "ofx_fno.cu", "ofx_setup.cu", "ofx_gnlse.cu"]
+SOURCES = ["ofx_api.cu", "ofx_k_heun_large.cu", "ofx_k_heun_small.cu", "ofx_k_rk23.cu", "ofx_k_heun_nee.cu", "ofx_noalloc.cu", "ofx_fp64.cu", "ofx_f32x2.cu", "ofx_gemm.cu", "ofx_fno.cu", "ofx_setup.cu", "ofx_gnlse.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "--expt-relaxed-constexpr", "-I" + os.path.join(HERE, "..", "include")]
+# per-file flags: the float-float kernel's error-free transformations must not be
+# contracted into fused multiply-adds (every intended one is an explicit fmaf)
+EXTRA_FLAGS = {"ofx_f32x2.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -48,7 +51,8 @@ def build(force: bool = False, verbose: bool = False, jobs: int = 0) -> str:
     objs = [os.path.join(OUT_DIR, os.path.splitext(s)[0] + ".o") for s in SOURCES]
 
     def compile_one(i):
-        cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, SOURCES[i]), "-o", objs[i]]
+        cmd = [nvcc] + NVCC_FLAGS + EXTRA_FLAGS.get(SOURCES[i], []) + ["-c", os.path.join(CSRC, SOURCES[i]),
+                                                                       "-o", objs[i]]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -429,9 +429,12 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
             "reached_steady_state": flat, "energies": energies, "field": sim.field}
 
 
-def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0=None) -> dict:
+def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0=None, trace_cap: int = 0) -> dict:
     """Round trips through the plain FP64 solver (optifax_propagate_fp64) with the
-    cavity transfer in FP64 on the host; returns seconds per trip."""
+    cavity transfer in FP64 on the host.  Timed with CUDA events on the launching
+    stream around all n_trips trips (the host transfer between passes included).
+    Returns seconds per trip, the first pass's crystal output (time domain,
+    complex128) and, with trace_cap > 0, its step trace."""
     from . import solver as sv
     a = opo.build_cavity(spec)
     si = a.si
@@ -440,15 +443,26 @@ def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0
     al, be, G = t64(si.alpha), t64(si.beta), t64(si.G)
     E = np.asarray(a.E0 if E0 is None else E0, dtype=np.complex128)
     attempts = 0
+    first_A = first_trace = None
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    for _ in range(n_trips):
-        A, st, _ = sv.propagate_fp64(torch.from_numpy(E).to(dev), al, be, G, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
-                                     dt=si.dt, n_steps=si.n_steps, max_err=si.max_err, min_err=si.min_err,
-                                     sel=si.sel)
+    ev0.record(stream)
+    for i in range(n_trips):
+        A, st, tr = sv.propagate_fp64(torch.from_numpy(E).to(dev), al, be, G, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                                      dt=si.dt, n_steps=si.n_steps, max_err=si.max_err, min_err=si.min_err,
+                                      sel=si.sel, trace_cap=trace_cap if i == 0 else 0)
         attempts += st["attempts"]
-        X = np.fft.fft(A.cpu().numpy())
+        A = A.cpu().numpy()
+        if i == 0:
+            first_A, first_trace = A, tr
+        X = np.fft.fft(A)
         E = np.fft.ifft(X * a.feedback + a.pump)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t0
-    return {"trips": n_trips, "wall_s": wall, "s_per_trip": wall / n_trips, "trips_per_s": n_trips / wall,
-            "attempts": attempts, "field": E}
+    gpu_s = ev0.elapsed_time(ev1) / 1000.0
+    return {"trips": n_trips, "wall_s": wall, "event_s": gpu_s, "s_per_trip": gpu_s / n_trips,
+            "trips_per_s": n_trips / gpu_s, "attempts": attempts, "field": E,
+            "first_pass_out": first_A, "first_pass_trace": first_trace}

@@ -1,13 +1,15 @@
-"""Precision study: one long chirped-crystal pass in FP32 (FP64 phase) and in full FP64.
+"""Precision study: one long chirped-crystal pass in FP32 (FP64 phase), in
+float-float and in full FP64.
 
 The workload is a 2^16-point sech^2 pump (100 fs, 3 W, 1040 nm) through a 20 mm
 MgO:PPLN crystal with a linearly chirped grating, period 28 -> 32 um
 (chirpedgrating.m with a = 1, tol 0.1 um), 2*10^5 solver steps of 0.1 um.  The
 FP32 propagator (optifax_propagate) runs it with its own adaptive schedule and
-again replaying the FP64 run's accept/reject decisions; the plain FP64 solver
-(optifax_propagate_fp64) is the FP64 reference at this size.  Each result
-reports the relative L2 field error, the relative pulse-energy error and the
-power-weighted RMS spectral phase error against the FP64 result.
+again replaying the FP64 run's accept/reject decisions; the float-float pass
+(optifax_propagate_f32x2) runs it with its own schedule from the FP64 input; the
+plain FP64 solver (optifax_propagate_fp64) is the FP64 reference at this size.
+Each result reports the relative L2 field error, the relative pulse-energy
+error and the power-weighted RMS spectral phase error against the FP64 result.
 """
 from __future__ import annotations
 
@@ -74,10 +76,12 @@ def _fp32_spec(si, e, dev, forced=None, trace_cap=0):
                         forced=None if forced is None else torch.from_numpy(forced.astype(np.int32)).to(dev))
 
 
-def run_fp64(si, e, dev, trace_cap=1 << 22):
-    """The FP64 pass; returns (field, stats, trace or None, seconds)."""
+def run_fp64(si, e, dev, trace_cap=1 << 22, entry="propagate_fp64"):
+    """The FP64 pass (or, with entry="propagate_f32x2", the float-float pass);
+    returns (field, stats, trace or None, seconds)."""
+    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    A, st, tr = sv.propagate_fp64(
+    A, st, tr = getattr(sv, entry)(
         torch.from_numpy(np.ascontiguousarray(e, dtype=np.complex128)).to(dev),
         torch.from_numpy(si.alpha.astype(np.float64)).to(dev), torch.from_numpy(si.beta.astype(np.float64)).to(dev),
         torch.from_numpy(si.G.astype(np.float64)).to(dev), w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, dt=si.dt,
@@ -108,11 +112,15 @@ def study(case: PrecisionCase = PrecisionCase(), device: int = 0) -> dict:
     # storing the input field in FP32 from the rounding during the pass
     e32 = e.astype(np.complex64).astype(np.complex128)
     a64q, st64q, _, _ = run_fp64(si, e32, dev, trace_cap=0)
+    a2, st2, tr2, t2 = run_fp64(si, e, dev, entry="propagate_f32x2")
+    same = tr2 is not None and tr2.shape == tr64.shape and bool(np.array_equal(tr2[:, :2], tr64[:, :2]))
     return {"case": dataclasses.asdict(case), "n_steps": si.n_steps,
             "fp64": {"attempts": st64["attempts"], "rejected": st64["rejected"], "seconds": t64,
                      "status": st64["status"]},
             "fp32": {"attempts": st32["attempts"], "rejected": st32["rejected"], "seconds": t32,
                      "status": st32["status"], **metrics(a32, a64)},
+            "f32x2": {"attempts": st2["attempts"], "rejected": st2["rejected"], "seconds": t2,
+                      "status": st2["status"], "schedule_identical": same, **metrics(a2, a64)},
             "fp32_replayed": {"attempts": st32r["attempts"], "seconds": t32r, "status": st32r["status"],
                               **metrics(a32r, a64)},
             "fp64_from_fp32_input": {"attempts": st64q["attempts"], **metrics(a64q, a64)},

@@ -187,15 +187,8 @@ def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int =
     return [p.out for p in pulses], stats
 
 
-@on_stream
-def propagate_fp64(E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
-                   variant: int = VARIANT_BATCH_XTAL, trace_cap: int = 0, stream=None):
-    """The plain full-FP64 crystal pass (optifax_propagate_fp64).
-
-    E: (B, N) or (N,) complex128 CUDA tensor; alpha, beta: (N,) float64; G: (S,)
-    or (B, S) float64.  Returns (A_out complex128 like E, stats dict, trace
-    ndarray (attempts, 3) or None).  All pulses share one schedule.
-    """
+def _propagate_wide(entry, E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
+                    variant, trace_cap, stream):
     E = _cuda(E, torch.complex128)
     squeeze = E.dim() == 1
     if squeeze:
@@ -212,18 +205,42 @@ def propagate_fp64(E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, m
     tr = (ctypes.c_int32 * (3 * trace_cap))() if trace_cap > 0 else None
     if stream is None:
         stream = torch.cuda.current_stream(E.device)
-    rc = lib.optifax_propagate_fp64(N, B, S, E.data_ptr(), out.data_ptr(), al.data_ptr(), be.data_ptr(),
-                                    G.data_ptr(), g_per_pulse, float(w0), float(bdiffw0), float(h), float(dt),
-                                    float(max_err), float(min_err), float(sel), int(variant),
-                                    ctypes.cast(tr, ctypes.c_void_p) if tr is not None else None,
-                                    int(trace_cap), ctypes.byref(st), int(stream.cuda_stream))
-    check(rc, None, "optifax_propagate_fp64")
+    rc = getattr(lib, entry)(N, B, S, E.data_ptr(), out.data_ptr(), al.data_ptr(), be.data_ptr(),
+                             G.data_ptr(), g_per_pulse, float(w0), float(bdiffw0), float(h), float(dt),
+                             float(max_err), float(min_err), float(sel), int(variant),
+                             ctypes.cast(tr, ctypes.c_void_p) if tr is not None else None,
+                             int(trace_cap), ctypes.byref(st), int(stream.cuda_stream))
+    check(rc, None, entry)
     stats = {f: getattr(st, f) for f, _ in nat.OptifaxPulseStats._fields_ if f != "reserved"}
     trace = None
     if tr is not None:
         n = min(stats["attempts"], trace_cap)
         trace = np.frombuffer(tr, dtype=np.int32).reshape(-1, 3)[:n].copy()
     return (out[0] if squeeze else out), stats, trace
+
+
+@on_stream
+def propagate_fp64(E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
+                   variant: int = VARIANT_BATCH_XTAL, trace_cap: int = 0, stream=None):
+    """The plain full-FP64 crystal pass (optifax_propagate_fp64).
+
+    E: (B, N) or (N,) complex128 CUDA tensor; alpha, beta: (N,) float64; G: (S,)
+    or (B, S) float64.  Returns (A_out complex128 like E, stats dict, trace
+    ndarray (attempts, 3) or None).  All pulses share one schedule.
+    """
+    return _propagate_wide("optifax_propagate_fp64", E, alpha, beta, G, w0=w0, bdiffw0=bdiffw0, h=h, dt=dt,
+                           n_steps=n_steps, max_err=max_err, min_err=min_err, sel=sel, variant=variant,
+                           trace_cap=trace_cap, stream=stream)
+
+
+@on_stream
+def propagate_f32x2(E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
+                    variant: int = VARIANT_BATCH_XTAL, trace_cap: int = 0, stream=None):
+    """The float-float crystal pass (optifax_propagate_f32x2): arguments and
+    results as propagate_fp64, field and transforms in float-float."""
+    return _propagate_wide("optifax_propagate_f32x2", E, alpha, beta, G, w0=w0, bdiffw0=bdiffw0, h=h, dt=dt,
+                           n_steps=n_steps, max_err=max_err, min_err=min_err, sel=sel, variant=variant,
+                           trace_cap=trace_cap, stream=stream)
 
 
 # ---------------------------------------------------------------------------

@@ -2,7 +2,9 @@
 
 Both compute in double precision from the same (FP32-valued) inputs, so the
 step schedules must be identical and the output fields agree to FP64 rounding
-of two different FFTs and sin/cos implementations: relative L2 <= 1e-11.
+of two different FFTs and sin/cos implementations: relative L2 <= 1e-11.  The
+cases cover every cluster shape of the persistent FP64 kernel (1 to 16 CTAs,
+512 to 65536 points) and its NEE_CPU.m instantiation.
 """
 import numpy as np
 import pytest
@@ -46,9 +48,10 @@ def _oracle(oracle, si, E, variant, G=None, shared=False):
                       g_per_pulse=G is not None, shared_schedule=shared, trace_cap=200000)
 
 
-@pytest.mark.parametrize("N,variant", [(1024, 0), (2048, 0), (1024, 2), (2048, 3), (512, 1), (1024, 5), (2048, 5)])
+@pytest.mark.parametrize("N,variant", [(1024, 0), (2048, 0), (1024, 2), (2048, 3), (512, 1), (1024, 5), (2048, 5),
+                                       (4096, 0), (8192, 2), (16384, 0), (16384, 5), (32768, 0), (65536, 3)])
 def test_fp64_single_pulse(oracle, N, variant):
-    win, si, E = make_case(N=N, length=0.2e-3, power=2.0)
+    win, si, E = make_case(N=N, length=0.2e-3 if N <= 2048 else 0.03e-3, power=2.0)
     A, st, tr = _fp64_gpu(si, E[0], variant)
     ref = _oracle(oracle, si, E[0], variant)
     assert st["status"] == 0
