@@ -732,8 +732,8 @@ def main():
         r64 = ff.fp64_plain_trips(spec, args.fp64_trips, device=local, E0=timed_input, trace_cap=4 * S)
         fp64 = {"trips_per_s": r64["trips_per_s"], "s_per_trip": r64["s_per_trip"], "trips": r64["trips"],
                 "attempts": r64["attempts"], "speedup_of_value": value / r64["trips_per_s"],
-                "note": "CUDA events around all trips; one kernel per sub-operation and a host flag "
-                        "read-back per attempt"}
+                "note": "CUDA events around all trips: the persistent FP64 kernel (one launch per pass, "
+                        "the field on a 16-CTA cluster), the cavity transfer on the host in FP64"}
         accuracy = accuracy_record(spec, timed_input, r64, device=local)
         # the same trips through the FP32 OPO kernel from the same input: next crystal input after each
         sim.field = torch.from_numpy(timed_input.astype(np.complex64)).to(dev)
