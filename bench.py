@@ -183,6 +183,34 @@ def cpu_oracle_sample(spec, fraction=0.05, threads=None, field=None, attempts_pe
                       f"({att} attempts, {el:.1f} s on {threads} thread{'s' if threads > 1 else ''}), {how}{cal}"}
 
 
+def cpu_replicas_sample(spec, field, fraction=0.01, cores=None):
+    """All host cores on independent copies of the cavity (one pass sample each, one
+    thread each, side by side; the oracle releases the GIL): the CPU's aggregate
+    round-trip throughput when it may spend every core on separate cavities.
+    Scaled to round trips by z-samples of the sample's own schedule."""
+    import concurrent.futures as cf
+    import numpy as np
+    from oracle import oracle as orc
+    from optifax_gb300.opo import build_cavity
+    cores = cores or host_cores()
+    si = build_cavity(spec).si
+    S = max(8, int(si.n_steps * fraction))
+
+    def one(_):
+        r = orc.run(field, si.alpha, si.G[:S], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=S, dt=si.dt,
+                    max_err=si.max_err, min_err=si.min_err, sel=float(np.ceil(S / 4)), nthreads=1)
+        return r.stats[0]["attempts"]
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        att = list(ex.map(one, range(cores)))
+    el = time.perf_counter() - t0
+    return {"value": cores * (S / si.n_steps) / el, "unit": UNIT, "cores": cores,
+            "sample": f"{cores} copies of the first {S} z-samples of one pass from the same input, one thread "
+                      f"each, side by side ({sum(att)} attempts in {el:.1f} s): aggregate round trips/s of "
+                      f"{cores} independent cavities"}
+
+
 def cpu_sweep_sample(insts, gpu_stats, cores, n_sample=16, fraction=0.02):
     """FP64 C oracle on a bounded sample of the sweep: the first `fraction` of the
     steps of `n_sample` instances spread over the list.  Cost per unit of
@@ -411,6 +439,32 @@ def pass_case(n_points: int, length: float, cta_points: int, reps: int = 2):
                           "attempts": st["attempts"], "ms": ms, "us_per_attempt": 1000 * ms / st["attempts"]}))
 
 
+def wide_case(n_points: int, length: float, entry: str, reps: int = 2):
+    """Profiling case: one crystal pass of the pass_case inputs through the wide-state
+    kernel (entry: fp64 or f32x2) run `reps` times; prints per-attempt time."""
+    import numpy as np
+    import torch
+    from optifax_gb300 import physics as ph, solver as sv
+    win = ph.SimWindow(1040e-9, n_points, n_points * 6e-12 / 2 ** 13)
+    si = ph.solver_inputs(ph.Crystal(length, 30e-6), win)
+    tau = min(200e-15, win.temporal_range / 12)
+    e = np.fft.fftshift(ph.sech_pump(win, 1040e-9, tau, 2.0) +
+                        ph.photon_noise(win, 0, mask=ph.window_transmission(win)))
+    e = np.fft.ifft(np.fft.fft(e) * np.sqrt(1.0 / si.n_index))
+    dev = torch.device("cuda:0")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    fn = sv.propagate_fp64 if entry == "fp64" else sv.propagate_f32x2
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, st, _ = fn(t(e), t(si.alpha.astype(np.float64)), t(si.beta.astype(np.float64)),
+                      t(si.G.astype(np.float64)), w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, dt=si.dt,
+                      n_steps=si.n_steps, max_err=si.max_err, min_err=si.min_err, sel=si.sel)
+        el = time.perf_counter() - t0
+        print(json.dumps({"case": "wide_pass", "entry": entry, "n_points": n_points, "length_m": length,
+                          "attempts": st["attempts"], "s": el, "us_per_attempt": 1e6 * el / st["attempts"]}))
+
+
 def fno_case(batch: int, reps: int = 3):
     """Profiling case: `reps` training steps (forward, backward, AdamW) of the
     surrogate network on synthetic data, batch x 6 x 4096; prints per-step device
@@ -629,12 +683,17 @@ def main():
                     help="profiling case: surrogate training steps at this batch size, no JSON bench line")
     ap.add_argument("--pass-case", default=None,
                     help="profiling case 'N,length_m': one crystal pass, run twice, no JSON bench line")
+    ap.add_argument("--wide-case", default=None,
+                    help="profiling case 'N,length_m,fp64|f32x2': one wide-state pass, run twice, no JSON line")
     args = ap.parse_args()
     if args.fno_case:
         return fno_case(args.fno_case)
     if args.pass_case:
         n, length = args.pass_case.split(",")
         return pass_case(int(n), float(length), args.cta_points)
+    if args.wide_case:
+        n, length, entry = args.wide_case.split(",")
+        return wide_case(int(n), float(length), entry)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -721,6 +780,7 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_oracle_sample(spec, fraction=0.05, field=timed_input,
                                 attempts_per_trip=attempts / K)
+        cpu["all_cores_independent_cavities"] = cpu_replicas_sample(spec, timed_input)
 
     # the plain full-FP64 GPU solver (optifax_propagate_fp64, host cavity transfer in
     # FP64) on the same crystal input as the timed window: the metric's comparator,
