@@ -236,6 +236,39 @@ def generate_raw(specs: List[opo.CavitySpec], n_trips: int, device: int = 0, gro
     return torch.cat(ins_all), torch.cat(outs_all), torch.cat(trip_idx), attempts
 
 
+def phase_aligned_err(pred: torch.Tensor, true: torch.Tensor, mask: torch.Tensor) -> float:
+    """min over a global phase phi of |pred e^{i phi} - true| / |true| on the masked bins.
+
+    The resonated signal of a singly resonant OPO has no reference phase (the idler
+    is not fed back, so the equations are invariant under a common rotation of the
+    signal), so two fields that differ only by a global signal phase describe the
+    same cavity state; the optimal phi is arg(sum conj(pred) true)."""
+    a, b = pred[mask].to(torch.complex128), true[mask].to(torch.complex128)
+    v = torch.sum(torch.conj(a) * b)
+    ph = v / v.abs() if float(v.abs()) > 0 else torch.ones((), dtype=torch.complex128, device=a.device)
+    return float((a * ph - b).abs().norm() / b.abs().norm().clamp_min(1e-300))
+
+
+def signal_mask(crop, n_points: int, device) -> torch.Tensor:
+    """Bins of the signal channels of an envelope crop (natural FFT order)."""
+    kc_s, lo_s, hi_s = crop.band[3], crop.band[4], crop.band[5]
+    m = torch.zeros(n_points, dtype=torch.bool, device=device)
+    m[(kc_s + torch.arange(lo_s, hi_s, device=device)) % n_points] = True
+    return m
+
+
+def align_signal_phase(ins: torch.Tensor, outs: torch.Tensor, mask: torch.Tensor) -> torch.Tensor:
+    """Targets with the trip's global signal-phase change removed: each output's
+    signal bins rotated so that their projection on the input's signal bins is real
+    and positive (pump bins untouched).  The network then learns the map up to the
+    signal's free phase, which is what the phase-aligned check compares."""
+    v = torch.sum(torch.conj(ins[:, mask]).to(torch.complex128) * outs[:, mask].to(torch.complex128), dim=1)
+    ph = torch.where(v.abs() > 0, torch.conj(v) / v.abs().clamp_min(1e-300), torch.ones_like(v))
+    out = outs.clone()
+    out[:, mask] = (outs[:, mask].to(torch.complex128) * ph[:, None]).to(outs.dtype)
+    return out
+
+
 def encode_pairs(ins: torch.Tensor, outs: torch.Tensor, crop, chunk: int = 1024):
     """Network inputs (P, 6, L) and targets (P, 4, L) of raw pairs (targets scaled
     with the input's sigma)."""
@@ -346,13 +379,15 @@ def _to_spec(E: torch.Tensor) -> torch.Tensor:
 
 def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips: int = 1000,
                      check_every: int = 10, check_tol: float = 0.05, finish_trips: int = 50,
-                     flat_tol: float = 1e-3, steady_tol: float = 1e-4, steady_trips: int = 10) -> dict:
+                     flat_tol: float = 1e-3, steady_tol: float = 1e-4, steady_trips: int = 10,
+                     phase_check: bool = True) -> dict:
     """max_trips round trips from sim's current state.
 
     Blocks of check_every trips: the first trip of a block is the check (the
     network's prediction and a solver pass from the same input; the cavity
     continues from the solver's result); when the relative L2 difference over the
-    fed-back band is within check_tol the other trips of the block run on the
+    fed-back band (after the best global signal phase, phase_aligned_err, unless
+    phase_check=False) is within check_tol the other trips of the block run on the
     network, otherwise on the solver.  The last finish_trips trips (and everything
     after the network's trips level out to flat_tol) run on the solver, which
     stops early once its steady-state test passes.  net=None runs the solver only.
@@ -382,7 +417,8 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
         energies.append(float(energy.item()))
         trips += 1
         sol_trips += 1
-        err = float(((Xs - Xt)[fbm]).abs().norm() / Xt[fbm].abs().norm().clamp_min(1e-30))
+        err = phase_aligned_err(Xs, Xt, fbm) if phase_check else \
+            float(((Xs - Xt)[fbm]).abs().norm() / Xt[fbm].abs().norm().clamp_min(1e-30))
         checks.append(err)
         n = min(check_every - 1, surrogate_until - trips)
         if n <= 0:

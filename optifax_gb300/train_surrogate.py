@@ -33,6 +33,10 @@ def main(argv=None):
     ap.add_argument("--check-tol", type=float, default=0.05)
     ap.add_argument("--fp64-trips", type=int, default=1)
     ap.add_argument("--out", default="surrogate_out")
+    ap.add_argument("--no-align", action="store_true",
+                    help="keep each target's global signal-phase change (default: remove it, as the check does)")
+    ap.add_argument("--weight-decay", type=float, default=0.0)
+    ap.add_argument("--power", default="0.5,3.0", help="pump power range of the training cavities [W]")
     args = ap.parse_args(argv)
     from . import fastforward as ff, opo
     from .surrogate import FNO
@@ -40,7 +44,8 @@ def main(argv=None):
     summary = {"args": vars(args), "runs": {}}
     base = opo.CavitySpec(crystal_length=args.crystal_length)
     t0 = time.perf_counter()
-    specs = ff.training_specs(args.cavities, seed=args.seed, base=base)
+    pw = tuple(float(x) for x in args.power.split(","))
+    specs = ff.training_specs(args.cavities, seed=args.seed, base=base, power=pw)
     ins, outs, trip_idx, attempts = ff.generate_raw(specs, args.trips)
     torch.cuda.synchronize()
     summary["generation"] = {"pairs": int(ins.shape[0]), "seconds": time.perf_counter() - t0,
@@ -48,10 +53,14 @@ def main(argv=None):
     print(json.dumps(summary["generation"]), flush=True)
     for rep in [r.strip() for r in args.repr.split(",") if r.strip()]:
         crop = ff.reference_env_crop(base) if rep == "env" else ff.reference_crop(base)
-        X, T = ff.encode_pairs(ins, outs, crop)
+        tgt = outs
+        if rep == "env" and not args.no_align:
+            tgt = ff.align_signal_phase(ins, outs, ff.signal_mask(crop, ins.shape[1], ins.device))
+        X, T = ff.encode_pairs(ins, tgt, crop)
         net = FNO(n_bins=crop.n_bins, max_batch=args.batch, seed=args.seed)
         hist = ff.train(net, X, T, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed,
-                        trip_idx=trip_idx, log=lambda s: print(f"[{rep}] {s}", flush=True))
+                        weight_decay=args.weight_decay, trip_idx=trip_idx,
+                        log=lambda s: print(f"[{rep}] {s}", flush=True))
         run = {"training": hist}
         print(json.dumps({"repr": rep, **{k: hist[k] for k in hist if k not in ("train_loss", "val_signal_rel_l2")}}),
               flush=True)

@@ -68,3 +68,32 @@ def test_interaction_picture_and_error_helpers():
     y[:, 2:4] *= 1.1                                              # signal channels 10 % off
     assert torch.allclose(ff.signal_rel_err(y, t), torch.full((3,), 0.1, dtype=t.dtype), atol=1e-12)
     assert torch.allclose(ff.sample_weights(t), 1.0 / t.pow(2).mean(dim=(1, 2)))
+
+
+def test_phase_aligned_error_ignores_a_global_signal_phase():
+    import torch
+    from optifax_gb300 import fastforward as ff
+    g = torch.Generator().manual_seed(0)
+    x = torch.randn(64, generator=g, dtype=torch.float64) + 1j * torch.randn(64, generator=g, dtype=torch.float64)
+    m = torch.zeros(64, dtype=torch.bool)
+    m[10:40] = True
+    assert ff.phase_aligned_err(x * complex(0.6, 0.8), x, m) < 1e-14
+    y = x.clone()
+    y[20] += 0.5
+    direct = float((x[m] - y[m]).abs().norm() / y[m].abs().norm())
+    assert abs(ff.phase_aligned_err(x, y, m) - direct) < 0.05 * direct
+
+
+def test_align_signal_phase_rotates_only_the_signal_bins():
+    import torch
+    from optifax_gb300 import fastforward as ff
+    g = torch.Generator().manual_seed(1)
+    ins = (torch.randn(3, 32, generator=g) + 1j * torch.randn(3, 32, generator=g)).to(torch.complex64)
+    m = torch.zeros(32, dtype=torch.bool)
+    m[4:20] = True
+    rot = torch.tensor([complex(0, 1), complex(-1, 0), complex(0.6, -0.8)], dtype=torch.complex64)
+    outs = ins.clone()
+    outs[:, m] = ins[:, m] * rot[:, None]
+    al = ff.align_signal_phase(ins, outs, m)
+    assert torch.allclose(al[:, m], ins[:, m], atol=1e-6)
+    assert torch.equal(al[:, ~m], outs[:, ~m])
