@@ -183,11 +183,12 @@ def cpu_oracle_sample(spec, fraction=0.05, threads=None, field=None, attempts_pe
                       f"({att} attempts, {el:.1f} s on {threads} thread{'s' if threads > 1 else ''}), {how}{cal}"}
 
 
-def cpu_replicas_sample(spec, field, fraction=0.01, cores=None):
+def cpu_replicas_sample(spec, field, attempts_per_trip, fraction=0.01, cores=None):
     """All host cores on independent copies of the cavity (one pass sample each, one
     thread each, side by side; the oracle releases the GIL): the CPU's aggregate
     round-trip throughput when it may spend every core on separate cavities.
-    Scaled to round trips by z-samples of the sample's own schedule."""
+    Scaled to round trips by attempts (attempts_per_trip, as the single-cavity
+    figure)."""
     import concurrent.futures as cf
     import numpy as np
     from oracle import oracle as orc
@@ -205,10 +206,11 @@ def cpu_replicas_sample(spec, field, fraction=0.01, cores=None):
     with cf.ThreadPoolExecutor(max_workers=cores) as ex:
         att = list(ex.map(one, range(cores)))
     el = time.perf_counter() - t0
-    return {"value": cores * (S / si.n_steps) / el, "unit": UNIT, "cores": cores,
+    per_attempt = el / (sum(att) / cores)          # wall time per attempt of each copy
+    return {"value": cores / (per_attempt * attempts_per_trip), "unit": UNIT, "cores": cores,
             "sample": f"{cores} copies of the first {S} z-samples of one pass from the same input, one thread "
-                      f"each, side by side ({sum(att)} attempts in {el:.1f} s): aggregate round trips/s of "
-                      f"{cores} independent cavities"}
+                      f"each, side by side ({sum(att)} attempts in {el:.1f} s), scaled by attempts "
+                      f"({attempts_per_trip:.0f} per trip): aggregate round trips/s of {cores} independent cavities"}
 
 
 def cpu_sweep_sample(insts, gpu_stats, cores, n_sample=16, fraction=0.02):
@@ -780,7 +782,7 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_oracle_sample(spec, fraction=0.05, field=timed_input,
                                 attempts_per_trip=attempts / K)
-        cpu["all_cores_independent_cavities"] = cpu_replicas_sample(spec, timed_input)
+        cpu["all_cores_independent_cavities"] = cpu_replicas_sample(spec, timed_input, attempts / K)
 
     # the plain full-FP64 GPU solver (optifax_propagate_fp64, host cavity transfer in
     # FP64) on the same crystal input as the timed window: the metric's comparator,

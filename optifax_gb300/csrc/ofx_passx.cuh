@@ -41,6 +41,8 @@ struct PulseX {
     optifax_pulse_stats* stats;
     void* cph;               // scratch: N carrier phasors exp(i w0 t_i) in R (written by the prologue)
     double* abc;             // scratch: N absorber factors
+    void* ztab;              // scratch: zcap z-carrier phasors exp(-i bdiffw0 h p), p = 0..zcap-1, in R
+    int zcap;
     uint64_t tau_theta;      // w0 dt in turns
     uint64_t tau_z;          // bdiffw0 h in turns (per z-sample)
     double w0, h, dt, max_err, min_err, sel, c_shock;
@@ -261,6 +263,11 @@ passx_kernel(const PulseX* __restrict__ pulses, XTables<R> tabs, KernelCfg cfg) 
         }
         Pd.abc[i] = f;
     }
+    // z-carrier phasor of every z-sample of the pass, shared by the cluster's CTAs
+    // (the FP64 sincospi leaves the per-stage path)
+    cplx* ztab = reinterpret_cast<cplx*>(Pd.ztab);
+    for (int pz = c * T + t; pz < Pd.zcap; pz += C * T)
+        ztab[pz] = X::from(turn_unit_d((uint64_t)0 - Pd.tau_z * (uint64_t)pz));
     if constexpr (C > 1) cg::this_cluster().sync(); else __syncthreads();
 
     const double h = Pd.h, sel = Pd.sel, Sd = (double)Pd.S, cs = Pd.c_shock;
@@ -320,7 +327,10 @@ passx_kernel(const PulseX* __restrict__ pulses, XTables<R> tabs, KernelCfg cfg) 
             {
                 cplx nl[P], L, Rr;
                 // ---- stage 1: K1 = f(A0) at z = k ----
-                cplx z = X::from(turn_unit_d((uint64_t)0 - Pd.tau_z * (uint64_t)(long long)kpos));
+                auto zphasor = [&](long long pz) -> cplx {
+                    return pz < Pd.zcap ? ztab[pz] : X::from(turn_unit_d((uint64_t)0 - Pd.tau_z * (uint64_t)pz));
+                };
+                cplx z = zphasor((long long)kpos);
                 nl_stage(a, z, nl, L, Rr);
                 // A1 = A0 + (K1/2 + K1/2) (MEX) or A0 + K1 (NEE_CPU.m:73); K1 kept in
                 // shared memory, A1 formed again where it is needed
@@ -332,7 +342,7 @@ passx_kernel(const PulseX* __restrict__ pulses, XTables<R> tabs, KernelCfg cfg) 
                 for (int j = 0; j < P; ++j)
                     bufK[P * t + j] = k_of(j == 0 ? L : nl[j - 1], nl[j], j == P - 1 ? Rr : nl[j + 1], hg, csr);
                 // ---- stage 2: K2 = f(A1) at z = k + stepmod ----
-                z = X::from(turn_unit_d((uint64_t)0 - Pd.tau_z * (uint64_t)(long long)(kpos + stepmod)));
+                z = zphasor((long long)(kpos + stepmod));
                 {
                     cplx a1[P];
 #pragma unroll

@@ -59,6 +59,8 @@ struct XWork {
     size_t cph_bytes = 0;
     double* abc = nullptr;
     size_t abc_bytes = 0;
+    void* ztab = nullptr;
+    size_t ztab_bytes = 0;
     PulseX* desc = nullptr;
     size_t desc_n = 0;
     int* trace = nullptr;
@@ -106,6 +108,8 @@ int passx_run(const std::vector<XKernel<R>>& kernels, XWork<R>& w, int n, int B,
     }
     if ((rc = grow_dev(&w.cph, &w.cph_bytes, sizeof(cplx) * (size_t)n * B))) return rc;
     if ((rc = grow_dev(&w.abc, &w.abc_bytes, sizeof(double) * (size_t)n * B))) return rc;
+    const int zcap = S + 64;     // z-samples k + stepmod of a pass stay below S + stepmod's clamp
+    if ((rc = grow_dev(&w.ztab, &w.ztab_bytes, sizeof(cplx) * (size_t)zcap * B))) return rc;
     size_t dn = w.desc_n * sizeof(PulseX);
     if ((rc = grow_dev(&w.desc, &dn, sizeof(PulseX) * (size_t)B))) return rc;
     w.desc_n = dn / sizeof(PulseX);
@@ -134,6 +138,8 @@ int passx_run(const std::vector<XKernel<R>>& kernels, XWork<R>& w, int n, int B,
         x.stats = (b == 0) ? w.stats : nullptr;
         x.cph = reinterpret_cast<cplx*>(w.cph) + (size_t)b * n;
         x.abc = w.abc + (size_t)b * n;
+        x.ztab = reinterpret_cast<cplx*>(w.ztab) + (size_t)b * zcap;
+        x.zcap = zcap;
         x.tau_theta = turns_fixed((long double)w0 * (long double)dt);
         x.tau_z = turns_fixed((long double)bdiffw0 * (long double)step_h);
         x.w0 = w0; x.h = step_h; x.dt = dt;
