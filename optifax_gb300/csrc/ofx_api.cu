@@ -593,7 +593,7 @@ extern "C" int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses
     int rc = OPTIFAX_OK;
     const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
     if (!twp) return rc;
-    const size_t need_k = (size_t)7 * M * n_pulses;
+    const size_t need_k = (size_t)8 * M * n_pulses;
     if (need_k > h->gnlse_k_cap) {
         size_t cap = h->gnlse_k_cap * sizeof(float2);
         rc = grow_scratch(h, (void**)&h->d_gnlse_k, &cap, need_k * sizeof(float2), st,
@@ -608,7 +608,7 @@ extern "C" int optifax_gnlse(optifax_handle h, const optifax_gnlse_pulse* pulses
         h->gnlse_desc_cap = cap / sizeof(GnlseDev);
         if (rc) return rc;
     }
-    for (int i = 0; i < n_pulses; ++i) d[(size_t)i].K = h->d_gnlse_k + (size_t)7 * M * i;
+    for (int i = 0; i < n_pulses; ++i) d[(size_t)i].K = h->d_gnlse_k + (size_t)8 * M * i;
     rc = order_after_previous(h, st);
     if (rc) return rc;
     cudaError_t e = cudaMemcpyAsync(h->d_gnlse_desc, d.data(), sizeof(GnlseDev) * (size_t)n_pulses,

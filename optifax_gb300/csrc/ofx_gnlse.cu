@@ -6,20 +6,28 @@
 //     AT = fft(AW e^{Lz}),  RS = dT fR fft(ifft(|AT|^2) RW),  L = iB - alpha/2,
 // in MATLAB's fft/ifft conventions (fft: exp(-i), ifft: exp(+i)/n), from
 // AW(0) = ifft(A).  The reference integrates it with MATLAB's ode45 (RelTol,
-// AbsTol, NormControl; gnlsefib.m:77-80); here an adaptive Dormand-Prince 5(4)
-// pair with the same tolerances and error norm,
+// AbsTol, NormControl; gnlsefib.m:77-80), outputs at linspace(0, L, n_saves).
+// Here: the Dormand-Prince 5(4) pair with the same tolerances and error norm,
 //     err = ||h sum_i e_i k_i|| / max(||y||, ||y_new||, AbsTol/RelTol) <= RelTol,
-// steps clamped to land on the save points (no interpolation), and positions
-// as integers in units of length / 2^40 so that every dispersion phase B_k z is
-// a 64-bit fixed-point product (exact mod one turn; only the final angle goes
+// under ode45's published step control (Shampine & Reichelt 1997): initial step
+// min(L/10, 0.8 RelTol^(1/5) max(||y0||, thr) / ||f0||), steps of at most L/10
+// stretched to the end when 1.1 h reaches it, a first failure scaling h by
+// max(0.1, 0.8 (RelTol/err)^(1/5)) and later ones halving it, growth by
+// min(5, 0.8 (RelTol/err)^(1/5)) only after a step that did not fail.  Steps do
+// not stop at the save points: a save point inside an accepted step is output
+// from a separate step of exactly that length from the step's start (its stages
+// reuse the accepted step's k1 and rows k2..k6; y_new waits in an eighth scratch
+// row).  Positions are integers in units of length / 2^40 so that every
+// dispersion phase B_k z is a 64-bit fixed-point product (exact mod one turn; only
+// the final angle goes
 // through FP32).  FP32 field arithmetic, norms reduced across the CTA in FP64
 // (per-thread partials of 16 modes in FP32), FP64 step control.
 //
 // Layout: the CTA's M/16 threads hold the spectral state y in registers, 16
 // modes each, in the FFT's bit-reversed slot order (slot s <-> mode bitrev(s));
 // the time-domain fields live in two padded shared-memory buffers; the seven
-// stage derivatives k_i sit in an L2-resident global scratch (7 x n per pulse,
-// each thread touching only its own 128-byte rows).  Each right-hand side costs
+// stage derivatives k_i and y_new sit in an L2-resident global scratch (8 x n per
+// pulse, each thread touching only its own 128-byte rows).  Each right-hand side costs
 // four in-place M-point transforms (two without Raman): MATLAB's fft of a
 // spectral array is conj(inverse(conj(.))), its ifft (1/n) conj(forward(conj(.))).
 #include <cmath>
@@ -192,43 +200,52 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
 #pragma unroll
     for (int j = 0; j < 16; ++j) y[j] = cscale(conjf2(v[j]), invM);
 
-    long long zc = 0, hc = 0, h = 0, target = 0;
+    long long zc = 0, hc = 0, h = 0, side_z = 0;
     int save_idx = 0, stage = 0, base = 0;
     int attempts = 0, accepted = 0, status = 0;
-    bool save_now = true;
-    double ny = 0.0;
+    bool nofailed = true, new_step = true, side = false;
+    double ny = 0.0, acc_nyn = 0.0, acc_err = 0.0;
     float hz = 0.f;
+    const long long nm1 = P.n_saves - 1;
+    auto save_point = [&](int i) -> long long { return ((long long)i * total + nm1 / 2) / nm1; };
+
+    // save `save_idx` from the spectral state src at position zp: AW e^{Lz}
+    // (fftshifted, x dT n) and AT = fft(AW e^{Lz})
+    auto do_save = [&](const float2 (&src)[16], long long zp) {
+        const float att = expf((float)(-0.5 * P.alpha * (double)zp * unit));
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int slot = 16 * t + j;
+            const float2 aw = cscale(cmul(src[j], turn_to_unit(rate_s[slot] * (uint64_t)zp)), att);
+            const int k = bitrev(slot, LOG2M);
+            P.AW_out[(size_t)save_idx * M + ((k + M / 2) & (M - 1))] = cscale(aw, awscale);
+            v[j] = conjf2(aw);
+        }
+        fft_inverse_from_regs<M>(bufA, tw1, tw2, t, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            P.AT_out[(size_t)save_idx * M + 16 * t + j] = conjf2(bufA[phys(16 * t + j)]);
+        ++save_idx;
+    };
+    do_save(y, 0);
 
     for (;;) {
-        if (save_now) {
-            // save `save_idx` at zc: AW e^{Lz} (fftshifted, x dT n) and AT = fft(AW e^{Lz})
-            const float att = expf((float)(-0.5 * P.alpha * (double)zc * unit));
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int slot = 16 * t + j;
-                const float2 aw = cscale(cmul(y[j], turn_to_unit(rate_s[slot] * (uint64_t)zc)), att);
-                const int k = bitrev(slot, LOG2M);
-                P.AW_out[(size_t)save_idx * M + ((k + M / 2) & (M - 1))] = cscale(aw, awscale);
-                v[j] = conjf2(aw);
-            }
-            fft_inverse_from_regs<M>(bufA, tw1, tw2, t, v);
-#pragma unroll
-            for (int j = 0; j < 16; ++j)
-                P.AT_out[(size_t)save_idx * M + 16 * t + j] = conjf2(bufA[phys(16 * t + j)]);
-            ++save_idx;
-            save_now = false;
-            if (save_idx == P.n_saves) break;
-        }
         // ---- stage input ys and its position zs ----
         long long zs = zc;
 #pragma unroll
         for (int j = 0; j < 16; ++j) ys[j] = y[j];
         if (stage > 0) {
-            if (stage == 1) {
-                // next save point: i total / (n_saves - 1), rounded half up
-                target = ((long long)save_idx * total + (P.n_saves - 1) / 2) / (P.n_saves - 1);
-                hc = h < target - zc ? h : target - zc;
+            if (stage == 1 && !side) {
+                if (new_step) {
+                    h = h > hmax ? hmax : (h < 1 ? 1 : h);
+                    hc = h;
+                    if (1.1 * (double)hc >= (double)(total - zc)) hc = total - zc;   // stretch to the end
+                    nofailed = true;
+                    new_step = false;
+                }
                 hz = (float)((double)hc * unit);
+            } else if (stage == 1) {
+                hz = (float)((double)(side_z - zc) * unit);
             }
             switch (stage) {
                 case 1: combine<1, 1>(ys, K, M, t, base, hz); break;
@@ -238,7 +255,7 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
                 case 5: combine<5, 5>(ys, K, M, t, base, hz); break;
                 default: combine<6, 6>(ys, K, M, t, base, hz); break;
             }
-            zs = zc + llrint(kDpC[stage] * (double)hc);
+            zs = zc + llrint(kDpC[stage] * (double)(side ? side_z - zc : hc));
         }
         // ---- right-hand side f(zs, ys) (gnlsefib.m:54-66) into v ----
         {
@@ -291,7 +308,7 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
                 kw[jj] = make_float4(v[2 * jj].x, v[2 * jj].y, v[2 * jj + 1].x, v[2 * jj + 1].y);
         }
         if (stage == 0) {
-            // initial step: 0.8 rtol^(1/5) max(||y||, thr) / ||f||
+            // initial step (ode45, NormControl): min(hmax, 0.8 rtol^(1/5) max(||y||, thr) / ||f||)
             double s2[2];
             block_sum2<T>(norm2_16(y), norm2_16(v), red, s2);
             ny = sqrt(s2[0]);
@@ -305,45 +322,101 @@ gnlse_kernel(const GnlseDev* __restrict__ pulses, const Twiddle* __restrict__ tw
             stage = 1;
             continue;
         }
-        if (stage < 6) { ++stage; continue; }
-
-        // ---- stage 6 done: ys = y_new, error estimate and decision ----
-        float2 ev[16];
+        bool finish = false;
+        if (side) {
+            if (stage < 5) { ++stage; continue; }
+            // stages k2..k6 of the step to the save point done: y(side_z) = y + h' sum a_7j k_j
 #pragma unroll
-        for (int j = 0; j < 16; ++j) ev[j] = make_float2(0.f, 0.f);
-        combine<-1, 7>(ev, K, M, t, base, hz);
-        double s2[2];
-        block_sum2<T>(norm2_16(ev), norm2_16(ys), red, s2);
-        const double errn = sqrt(s2[0]), nyn = sqrt(s2[1]);
-        const double err = errn / fmax(fmax(ny, nyn), thr);
-        const bool ok = err <= P.rtol;
-        if (t == 0 && P.trace && attempts < P.trace_cap) {
-            P.trace[2 * attempts] = hc;
-            P.trace[2 * attempts + 1] = ok ? 1 : 0;
+            for (int j = 0; j < 16; ++j) ys[j] = y[j];
+            combine<6, 6>(ys, K, M, t, base, hz);
+            do_save(ys, side_z);
+            if (save_idx < P.n_saves && save_point(save_idx) < zc + hc) {
+                side_z = save_point(save_idx);
+                stage = 1;
+                continue;
+            }
+            // back to the accepted step: y_new from the stash row
+            const float4* sr = krow(K, M, 7, t);
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+                const float4 w = sr[jj];
+                ys[2 * jj] = make_float2(w.x, w.y);
+                ys[2 * jj + 1] = make_float2(w.z, w.w);
+            }
+            side = false;
+            finish = true;
+        } else {
+            if (stage < 6) { ++stage; continue; }
+
+            // ---- stage 6 done: ys = y_new, error estimate and decision ----
+            float2 ev[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) ev[j] = make_float2(0.f, 0.f);
+            combine<-1, 7>(ev, K, M, t, base, hz);
+            double s2[2];
+            block_sum2<T>(norm2_16(ev), norm2_16(ys), red, s2);
+            const double errn = sqrt(s2[0]), nyn = sqrt(s2[1]);
+            const double err = errn / fmax(fmax(ny, nyn), thr);
+            const bool ok = err <= P.rtol;
+            if (t == 0 && P.trace && attempts < P.trace_cap) {
+                P.trace[2 * attempts] = hc;
+                P.trace[2 * attempts + 1] = ok ? 1 : 0;
+            }
+            ++attempts;
+            if (!isfinite(errn) || !isfinite(nyn)) { status |= OPTIFAX_PULSE_NAN; break; }
+            if (ok) {
+                ++accepted;
+                acc_err = err;
+                acc_nyn = nyn;
+                if (save_idx < P.n_saves && save_point(save_idx) < zc + hc) {
+                    // a save point inside the step: stash y_new, then a step of exactly that length
+                    float4* sw = reinterpret_cast<float4*>(K + (size_t)7 * M + 16 * t);
+#pragma unroll
+                    for (int jj = 0; jj < 8; ++jj)
+                        sw[jj] = make_float4(ys[2 * jj].x, ys[2 * jj].y, ys[2 * jj + 1].x, ys[2 * jj + 1].y);
+                    side = true;
+                    side_z = save_point(save_idx);
+                    stage = 1;
+                    continue;
+                }
+                finish = true;
+            } else {
+                // a failed step: the first failure scales by max(0.1, 0.8 (rtol/err)^(1/5)),
+                // later ones halve (the factor only scales an integer step: FP32 powf serves)
+                if (nofailed) {
+                    nofailed = false;
+                    const float errf = (float)err;
+                    const double fac = (double)fmaxf(0.1f, 0.8f * powf((float)P.rtol / errf, 0.2f));
+                    const long long hi = (long long)((double)hc * fac);
+                    hc = hi < 1 ? 1 : hi;
+                } else {
+                    hc = hc / 2 < 1 ? 1 : hc / 2;
+                }
+                if (attempts >= P.max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; break; }
+                stage = 1;
+                continue;
+            }
         }
-        ++attempts;
-        if (!isfinite(errn) || !isfinite(nyn)) { status |= OPTIFAX_PULSE_NAN; break; }
-        // step factor 0.8 (RelTol/err)^(1/5): it only scales the next integer step, so FP32
-        // powf serves (an error ratio beyond FP32's range gives inf, clamped to 5 below)
-        const float errf = (float)err;
-        const double fac = errf == 0.f ? 5.0 : (double)(0.8f * powf((float)P.rtol / errf, 0.2f));
-        if (ok) {
-            ++accepted;
+        if (finish) {
             zc += hc;
 #pragma unroll
             for (int j = 0; j < 16; ++j) y[j] = ys[j];
-            ny = nyn;
+            ny = acc_nyn;
             base = (base + 6) % 7;                          // FSAL: k7 becomes the next k1
-            const double hh = (double)hc * fmin(5.0, fac);
-            const long long hi = hh >= (double)hmax ? hmax : (long long)hh;
-            h = hi < 1 ? 1 : hi;
-            if (zc == target) save_now = true;
-        } else {
-            const long long hi = (long long)((double)hc * fmax(0.1, fmin(1.0, fac)));
-            h = hi < 1 ? 1 : hi;
+            if (save_idx < P.n_saves && save_point(save_idx) == zc) do_save(y, zc);
+            if (save_idx >= P.n_saves || zc >= total) break;
+            // growth after a step with no failure: h / (1.25 (err/rtol)^(1/5)), at most 5 h
+            if (nofailed) {
+                const float ratio = (float)(acc_err / P.rtol);
+                const float temp = 1.25f * powf(ratio, 0.2f);
+                h = temp > 0.2f ? (long long)((double)hc / (double)temp) : 5 * hc;
+            } else {
+                h = hc;
+            }
+            new_step = true;
+            if (attempts >= P.max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; break; }
+            stage = 1;
         }
-        if (attempts >= P.max_attempts) { status |= OPTIFAX_PULSE_ATTEMPT_LIMIT; break; }
-        stage = 1;
     }
     if (t == 0 && P.stats) {
         optifax_gnlse_stats st;

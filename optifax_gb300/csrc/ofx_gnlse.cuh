@@ -18,7 +18,7 @@ struct GnlseDev {
     float2* AW_out;           // n_saves x n
     long long* trace;         // 2 per attempt
     optifax_gnlse_stats* stats;
-    float2* K;                // scratch: 7 x n stage derivatives (slot order)
+    float2* K;                // scratch: 8 x n (seven stage derivatives, then y_new; slot order)
     double gamma, fr, dT, alpha, length, rtol, atol;
     int n_saves, trace_cap, max_attempts, pad;
 };

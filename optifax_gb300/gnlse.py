@@ -8,7 +8,10 @@ AW: fftshifted spectral field x dT n, W: absolute angular-frequency grid).  The
 operators (gnlsefib.m:22-50) are set up here in FP64; the propagation itself runs in
 the sm_103a kernel behind ``optifax_gnlse`` (csrc/ofx_gnlse.cu): an adaptive
 Dormand-Prince 5(4) pair with the tolerances the reference gives ode45 (RelTol
-1e-5, AbsTol 1e-12, NormControl), steps landing on the save points.
+1e-5, AbsTol 1e-12, NormControl) under ode45's published step control (initial
+step, first-failure scaling then halving, growth only after a step without
+failure, steps of at most a tenth of the fibre stretched to its end); save points
+inside a step are output by a separate step of exactly that length.
 """
 from __future__ import annotations
 

@@ -10,14 +10,21 @@
  * AW obeys dAW/dz = i gamma W ifft(AT ((1 - fR)|AT|^2 + RS)) e^{-Lz} with
  * AT = fft(AW e^{Lz}), RS = dT fR fft(ifft(|AT|^2) RW) and L = i B - alpha/2, in
  * MATLAB's (and NumPy's) fft/ifft conventions, from AW(0) = ifft(A).
- * gnlsefib.m:77-80 integrates it with MATLAB's ode45 (a closed binary); this file
- * follows the scheme that oracle/gnlse_oracle.py and the GPU kernel share: the
- * Dormand-Prince 5(4) pair (FSAL), NormControl error norm
- * err = ||h sum_i e_i k_i|| / max(||y||, ||y_new||, AtolRtol), accept when
- * err <= RelTol, step factor min(5, max(0.1, 0.8 (RelTol/err)^(1/5))) (no growth
- * after a rejection), steps at most a tenth of the fibre and clamped to the save
- * points, positions as integers in units of length / 2^40.  Outputs as
- * gnlsefib.m:82-89.  Independent pulses run in parallel (OpenMP).
+ * gnlsefib.m:70-80 integrates it with MATLAB's ode45 (a closed binary) and outputs at
+ * linspace(0, length, n_saves).  This file follows the step control that
+ * oracle/gnlse_oracle.py and the GPU kernel share, restated from ode45's published
+ * algorithm (Shampine & Reichelt, "The MATLAB ODE Suite", 1997): the Dormand-Prince
+ * 5(4) pair (FSAL), NormControl error norm err = ||h sum_i e_i k_i|| /
+ * max(||y||, ||y_new||, AbsTol/RelTol), accepted when err <= RelTol; initial step
+ * min(hmax, 0.8 RelTol^(1/5) max(||y0||, threshold) / ||f0||); hmax = length / 10;
+ * a step stretched to the end when 1.1 h reaches it; after a failure h scales by
+ * max(0.1, 0.8 (RelTol/err)^(1/5)) the first time and halves after that; after an
+ * accepted step with no failure h /= 1.25 (err/RelTol)^(1/5) (h *= 5 when that
+ * divisor is <= 0.2), after one that failed first h is kept.  Steps do not stop at
+ * the save points: a save point inside an accepted step is output from a separate
+ * Dormand-Prince step of exactly that length from the step's start.  Positions are
+ * integers in units of length / 2^40.  Outputs as gnlsefib.m:82-89.  Independent
+ * pulses run in parallel (OpenMP).
  *
  * Parity with MATLAB's own ode45 output is unpinned; this restatement is checked
  * against the NumPy one (tests/test_gnlse_oracle.py) and the known answers there.
@@ -133,15 +140,43 @@ static void rhs(const ofx_gnlse_params* p, const double* B, const double* W, con
 }
 
 /* save i at position zc (units): AT = fft(AW e^{Lz}), AW e^{Lz} fftshifted x dT n */
-static void save(const ofx_gnlse_params* p, const double* B, gwork* w, int i, long long zc, double unit,
-                 double* AT_out, double* AW_out) {
+static void save(const ofx_gnlse_params* p, const double* B, gwork* w, const cplx* y, int i, long long zc,
+                 double unit, double* AT_out, double* AW_out) {
     const int n = p->n;
     cplx* at = (cplx*)AT_out + (size_t)i * n;
     cplx* aw = (cplx*)AW_out + (size_t)i * n;
     lz(p, B, (double)zc * unit, w->e);
-    for (int k = 0; k < n; ++k) at[k] = cmul(w->y[k], w->e[k]);
+    for (int k = 0; k < n; ++k) at[k] = cmul(y[k], w->e[k]);
     for (int k = 0; k < n; ++k) aw[k] = cscale(cscale(at[(k + n / 2) % n], p->dT), (double)n);
     fft_exec(&w->plan, at, 0);
+}
+
+/* save point i: i total / (n_saves - 1), rounded half up */
+static long long save_point(int i, long long total, long long nm1) { return ((long long)i * total + nm1 / 2) / nm1; }
+
+/* stages 2..last+1 of a Dormand-Prince step of hc units from (zc, y) with k[0] = k1
+ * given, into k[1..last]; out = the 5th-order value y + h sum a_7j k_j (its k_7 is
+ * computed only when last == 6) */
+static void dp_stages(const ofx_gnlse_params* p, const double* B, const double* W, const cplx* RW, gwork* w,
+                      cplx* const* k, long long zc, long long hc, double unit, int last, cplx* out) {
+    const int n = p->n;
+    const double hz = (double)hc * unit;
+    for (int s = 1; s <= last; ++s) {
+        for (int i = 0; i < n; ++i) {
+            cplx a = cmk(0.0, 0.0);
+            for (int j = 0; j < s; ++j)
+                if (DP_A[s][j] != 0.0) a = cadd(a, cscale(k[j][i], DP_A[s][j]));
+            w->ys[i] = cadd(w->y[i], cscale(a, hz));
+        }
+        const long long zs = zc + (long long)nearbyint(DP_C[s] * (double)hc);
+        rhs(p, B, W, RW, w, (double)zs * unit, w->ys, k[s]);
+    }
+    for (int i = 0; i < n; ++i) {
+        cplx a = cmk(0.0, 0.0);
+        for (int j = 0; j < 6; ++j)
+            if (DP_A[6][j] != 0.0) a = cadd(a, cscale(k[j][i], DP_A[6][j]));
+        out[i] = cadd(w->y[i], cscale(a, hz));
+    }
 }
 
 static int run_one(const ofx_gnlse_params* p, const cplx* A, const double* B, const double* W, const cplx* RW,
@@ -159,7 +194,8 @@ static int run_one(const ofx_gnlse_params* p, const cplx* A, const double* B, co
     fft_exec(&w.plan, w.y, 1);
     for (int i = 0; i < n; ++i) w.y[i] = cscale(w.y[i], 1.0 / (double)n);
     long long zc = 0;
-    save(p, B, &w, 0, 0, unit, AT_out, AW_out);
+    save(p, B, &w, w.y, 0, 0, unit, AT_out, AW_out);
+    int si = 1;
     int f = 0;
     rhs(p, B, W, RW, &w, 0.0, w.y, w.buf[f]);
     double ny = norm(w.y, n);
@@ -171,58 +207,67 @@ static int run_one(const ofx_gnlse_params* p, const cplx* A, const double* B, co
         h = !(hh < (double)hmax) ? hmax : (hh < 1.0 ? 1 : (long long)hh);   /* NaN: hmax */
     }
     int att = 0, acc = 0, fi = 0;
-    for (int si = 1; si < p->n_saves && rc == 0; ++si) {
-        const long long target = ((long long)si * total + nm1 / 2) / nm1;   /* i total / (n_saves - 1), half up */
-        while (zc < target) {
-            long long hc = h < target - zc ? h : target - zc;
+    while (zc < total && rc == 0) {
+        h = h > hmax ? hmax : (h < 1 ? 1 : h);
+        long long hc = h;
+        if (1.1 * (double)hc >= (double)(total - zc)) hc = total - zc;    /* stretch to the end */
+        int nofailed = 1;
+        double err = 0.0, nyn = 0.0;
+        cplx* k[7];
+        for (int s_ = 0; s_ < 7; ++s_) k[s_] = w.buf[(f + s_) % 7];
+        for (;;) {
             if (forced) {
                 if (fi >= n_forced) { rc = -3; break; }
                 hc = forced[2 * fi];
             }
+            dp_stages(p, B, W, RW, &w, k, zc, hc, unit, 6, w.ynew);
             const double hz = (double)hc * unit;
-            cplx* k[7];
-            for (int s = 0; s < 7; ++s) k[s] = w.buf[(f + s) % 7];
-            for (int s = 1; s < 7; ++s) {
-                for (int i = 0; i < n; ++i) {
-                    cplx a = cmk(0.0, 0.0);
-                    for (int j = 0; j < s; ++j)
-                        if (DP_A[s][j] != 0.0) a = cadd(a, cscale(k[j][i], DP_A[s][j]));
-                    w.ys[i] = cadd(w.y[i], cscale(a, hz));
-                }
-                const long long zs = zc + (long long)nearbyint(DP_C[s] * (double)hc);
-                rhs(p, B, W, RW, &w, (double)zs * unit, w.ys, k[s]);
-            }
             for (int i = 0; i < n; ++i) {
-                cplx a = cmk(0.0, 0.0), e = cmk(0.0, 0.0);
-                for (int j = 0; j < 6; ++j)
-                    if (DP_A[6][j] != 0.0) a = cadd(a, cscale(k[j][i], DP_A[6][j]));
+                cplx e = cmk(0.0, 0.0);
                 for (int j = 0; j < 7; ++j)
                     if (DP_E[j] != 0.0) e = cadd(e, cscale(k[j][i], DP_E[j]));
-                w.ynew[i] = cadd(w.y[i], cscale(a, hz));
                 w.acc[i] = cscale(e, hz);
             }
-            const double nyn = norm(w.ynew, n);
-            const double err = norm(w.acc, n) / fmax(fmax(ny, nyn), thr);
+            nyn = norm(w.ynew, n);
+            err = norm(w.acc, n) / fmax(fmax(ny, nyn), thr);
             if (!isfinite(err) || att >= MAX_ATTEMPTS) { rc = isfinite(err) ? -5 : -4; break; }
             int ok = err <= p->rtol;
             if (forced) { ok = forced[2 * fi + 1] != 0; ++fi; }
             if (trace && att < trace_cap) { trace[2 * att] = hc; trace[2 * att + 1] = ok; }
             ++att;
-            const double fac = err == 0.0 ? 5.0 : 0.8 * pow(p->rtol / err, 0.2);
-            if (ok) {
-                ++acc;
-                zc += hc;
-                cplx* t = w.y; w.y = w.ynew; w.ynew = t;
-                f = (f + 6) % 7;                                        /* FSAL: k_7 is the next k_1 */
-                ny = nyn;
-                const long long hi = (long long)((double)hc * fmin(5.0, fac));
-                h = hi > hmax ? hmax : (hi < 1 ? 1 : hi);
+            if (ok) break;
+            if (nofailed) {
+                nofailed = 0;
+                const long long hi = (long long)((double)hc * fmax(0.1, 0.8 * pow(p->rtol / err, 0.2)));
+                hc = hi < 1 ? 1 : hi;
             } else {
-                const long long hi = (long long)((double)hc * fmax(0.1, fmin(1.0, fac)));
-                h = hi < 1 ? 1 : hi;
+                hc = hc / 2 < 1 ? 1 : hc / 2;
             }
         }
-        if (rc == 0) save(p, B, &w, si, zc, unit, AT_out, AW_out);
+        if (rc) break;
+        ++acc;
+        /* save points inside the step: a separate step of exactly that length from zc
+           (stages k2..k6 overwrite the accepted step's, which are not needed again) */
+        while (si < p->n_saves && save_point(si, total, nm1) < zc + hc) {
+            const long long sp = save_point(si, total, nm1);
+            dp_stages(p, B, W, RW, &w, k, zc, sp - zc, unit, 5, w.ys);
+            save(p, B, &w, w.ys, si, sp, unit, AT_out, AW_out);
+            ++si;
+        }
+        zc += hc;
+        cplx* t = w.y; w.y = w.ynew; w.ynew = t;
+        f = (f + 6) % 7;                                                /* FSAL: k_7 is the next k_1 */
+        ny = nyn;
+        if (si < p->n_saves && save_point(si, total, nm1) == zc) {
+            save(p, B, &w, w.y, si, zc, unit, AT_out, AW_out);
+            ++si;
+        }
+        if (nofailed) {
+            const double temp = 1.25 * pow(err / p->rtol, 0.2);
+            h = temp > 0.2 ? (long long)((double)hc / temp) : 5 * hc;
+        } else {
+            h = hc;
+        }
     }
     *attempts_out = att;
     *accepted_out = acc;

@@ -11,17 +11,31 @@ W = V + w0 with gamma/w0 when a shock frequency is given, RW = n ifft(fftshift(h
 in MATLAB's fft/ifft conventions (fft: exp(-i ...), ifft: exp(+i ...) / n).
 
 gnlsefib.m integrates with MATLAB's ode45 (RelTol 1e-5, AbsTol 1e-12, NormControl
-on, gnlsefib.m:77-80), a closed third-party binary.  This oracle and the GPU kernel
-instead share one published scheme: the Dormand-Prince 5(4) pair (FSAL) with the
-same tolerances and NormControl error norm, err = ||h sum e_i k_i||_2 /
-max(||y||_2, ||y_new||_2, AbsTol/RelTol), accept when err <= RelTol, the standard
-controller h *= min(5, max(0.1, 0.8 (RelTol/err)^(1/5))) (no growth after a
-rejection), steps at most a tenth of the fibre and clamped to land on the save
-points (so no dense-output interpolation).  Positions are integers in a unit of
-flength / 2^40, so the GPU and the oracle evaluate at identical z; the oracle can
-replay the GPU's (step, accept) sequence so that the comparison is arithmetic only.
-Parity with MATLAB's own ode45 is not claimed (unpinned): both integrate the same
-ODE to the same tolerance.
+on, outputs at linspace(0, flength, nsaves); gnlsefib.m:70-80).  ode45 itself is a
+closed binary; its algorithm is published (Shampine & Reichelt, "The MATLAB ODE
+Suite", SIAM J. Sci. Comput. 18(1), 1997) and restated here, shared by this oracle,
+the C restatement and the GPU kernel:
+  * the Dormand-Prince 5(4) pair (FSAL), NormControl error norm
+    err = ||h sum e_i k_i||_2 / max(||y||_2, ||y_new||_2, AbsTol/RelTol), accepted
+    when err <= RelTol;
+  * initial step: h = min(hmax, span), reduced to 1/rh when h rh > 1, with
+    rh = (||f0|| / max(||y0||, threshold)) / (0.8 RelTol^(1/5));
+  * hmax = span / 10 (MaxStep's default); before each step the step is stretched
+    to the end of the span when 1.1 h >= the remaining length;
+  * after a failed step: the first failure of the step scales h by
+    max(0.1, 0.8 (RelTol/err)^(1/5)), later ones halve it;
+  * after an accepted step with no failure: h /= 1.25 (err/RelTol)^(1/5) when that
+    divisor exceeds 0.2, else h *= 5; after a step that failed first, h is kept;
+  * the steps do not stop at the save points: a save point inside an accepted step
+    is output from a separate Dormand-Prince step of exactly that length from the
+    step's start (5th order; MATLAB interpolates with its 4th-order continuous
+    extension instead, so saved values inside a step differ from MATLAB's by the
+    order of the local error, while the step sequence is ode45's).
+Positions are integers in a unit of flength / 2^40 (hmin = 1 unit), so the GPU and
+the oracle evaluate at identical z; the oracle can replay the GPU's (step, accept)
+sequence so that the comparison is arithmetic only.  Parity with MATLAB's own ode45
+output is not claimed (no MATLAB): the step-control rules are restated from the
+publication, not compared with a MATLAB run.
 """
 from __future__ import annotations
 
@@ -117,6 +131,19 @@ class GnlseResult:
     accepted: int
 
 
+def _dp_step(ops: GnlseOps, y, f, zc, hc, unit, last_stage=6):
+    """Stages of one Dormand-Prince step of hc units from (zc, y) with k1 = f: returns
+    (the 5th-order value, [k1..k7] or [k1..k6] when last_stage == 5)."""
+    hz = hc * unit
+    k = [f]
+    for s in range(1, last_stage + 1):
+        ys = y + hz * sum(DP_A[s][j] * k[j] for j in range(s) if DP_A[s][j] != 0.0)
+        zs = (zc + int(round(DP_C[s] * hc))) * unit
+        k.append(rhs(ops, zs, ys))
+    ynew = y + hz * sum(DP_A[6][j] * k[j] for j in range(6) if DP_A[6][j] != 0.0)
+    return ynew, k
+
+
 def propagate(ops: GnlseOps, A, flength, nsaves, rtol=1e-5, atol=1e-12, forced=None) -> GnlseResult:
     """Integrate from z = 0 to flength, saving at linspace(0, flength, nsaves).
     forced: optional sequence of (h_count, accepted) replacing the step control."""
@@ -138,30 +165,31 @@ def propagate(ops: GnlseOps, A, flength, nsaves, rtol=1e-5, atol=1e-12, forced=N
         out_aw[i] = np.fft.fftshift(aw) * ops.dT * n
 
     save(0, 0, y)
+    si = 1
     f = rhs(ops, 0.0, y)
     ny = np.linalg.norm(y)
     nf = np.linalg.norm(f)
-    # initial step: the error-per-step estimate 0.8 rtol^(1/5) max(||y||, thr) / ||f||
-    h = hmax if nf == 0.0 else min(hmax, max(1, int((0.8 * rtol ** 0.2) * max(ny, thr) / nf / unit)))
+    # initial step (ode45, NormControl): min(hmax, span), 1/rh when h rh > 1
+    h = hmax
+    rh = (nf / max(ny, thr)) / (0.8 * rtol ** 0.2)
+    if h * unit * rh > 1.0:
+        h = max(1, int(1.0 / rh / unit))
     steps = []
     att = acc = 0
     fi = 0
-    for si in range(1, len(saves)):
-        target = saves[si]
-        while zc < target:
-            hc = min(h, target - zc)
+    while zc < total:
+        h = min(hmax, max(1, h))
+        hc = h
+        if 1.1 * hc >= total - zc:
+            hc = total - zc                      # stretch to the end of the span
+        nofailed = True
+        while True:
             if forced is not None:
                 if fi >= len(forced):
                     raise RuntimeError("forced schedule exhausted")
                 hc = int(forced[fi][0])
-            hz = hc * unit
-            k = [f]
-            for s in range(1, 7):
-                ys = y + hz * sum(DP_A[s][j] * k[j] for j in range(s) if DP_A[s][j] != 0.0)
-                zs = (zc + int(round(DP_C[s] * hc))) * unit
-                k.append(rhs(ops, zs, ys))
-            ynew = y + hz * sum(DP_A[6][j] * k[j] for j in range(6) if DP_A[6][j] != 0.0)
-            errv = hz * sum(DP_E[j] * k[j] for j in range(7) if DP_E[j] != 0.0)
+            ynew, k = _dp_step(ops, y, f, zc, hc, unit)
+            errv = (hc * unit) * sum(DP_E[j] * k[j] for j in range(7) if DP_E[j] != 0.0)
             nyn = np.linalg.norm(ynew)
             err = np.linalg.norm(errv) / max(ny, nyn, thr)
             ok = err <= rtol
@@ -170,15 +198,30 @@ def propagate(ops: GnlseOps, A, flength, nsaves, rtol=1e-5, atol=1e-12, forced=N
                 fi += 1
             steps.append((hc, int(ok)))
             att += 1
-            fac = 5.0 if err == 0.0 else 0.8 * (rtol / err) ** 0.2
             if ok:
-                acc += 1
-                zc += hc
-                y, f, ny = ynew, k[6], nyn
-                h = min(hmax, max(1, int(hc * min(5.0, fac))))
+                break
+            if nofailed:
+                nofailed = False
+                fac = 0.1 if not np.isfinite(err) else max(0.1, 0.8 * (rtol / err) ** 0.2)
+                hc = max(1, int(hc * fac))
             else:
-                h = max(1, int(hc * max(0.1, min(1.0, fac))))
-        save(si, zc, y)
+                hc = max(1, hc // 2)
+        acc += 1
+        # save points inside the step: a separate step of exactly that length from zc
+        while si < nsaves and saves[si] < zc + hc:
+            ys, _ = _dp_step(ops, y, f, zc, saves[si] - zc, unit, last_stage=5)
+            save(si, saves[si], ys)
+            si += 1
+        zc += hc
+        y, f, ny = ynew, k[6], nyn
+        if si < nsaves and saves[si] == zc:
+            save(si, zc, y)
+            si += 1
+        if nofailed:
+            temp = 1.25 * (err / rtol) ** 0.2
+            h = int(hc / temp) if temp > 0.2 else 5 * hc
+        else:
+            h = hc
     Z = np.array([s * unit for s in saves])
     return GnlseResult(Z=Z, AT=out_at, AW=out_aw, steps=steps, attempts=att, accepted=acc)
 

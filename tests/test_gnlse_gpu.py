@@ -99,6 +99,34 @@ def test_gnlse_matches_oracle_on_gpu_schedule(n, window, loss, L):
     assert abs(ref_ph[-1] / ref_ph[0] / expect - 1) < 2e-7 * st["attempts"], info
 
 
+def test_gnlse_schedule_follows_ode45_rules():
+    """The GPU's own step sequence against the oracle's restatement of ode45's step
+    control: the same attempts and accept/reject decisions, step sizes equal to the
+    FP32 step factor's rounding (1e-5 relative), and steps that run through the save
+    points instead of stopping at them."""
+    n, window, L, nsaves = 2048, 4e-12, 0.08, 5
+    T = _grid(n, window)
+    w0 = 2 * np.pi * C0 / 835e-9
+    A = np.sqrt(1000.0) / np.cosh(T / T0)
+    RT = go.raman_response(T)
+    r, st, steps = _run_gpu(T, A, w0, BETAS, 0.0, 0.18, RT, L, nsaves)
+    ops = go.gnlse_ops(T, w0, GAMMA, BETAS, 0.0, 0.18, RT)
+    own = go.propagate(ops, np.asarray(A, np.complex64).astype(np.complex128), L, nsaves)
+    assert st["status"] == 0 and len(steps) == own.attempts
+    g = np.array(steps, dtype=np.float64)
+    o = np.array(own.steps, dtype=np.float64)
+    assert np.array_equal(g[:, 1], o[:, 1])
+    assert np.max(np.abs(g[:, 0] - o[:, 0]) / o[:, 0]) < 1e-5
+    total = 1 << go.Z_BITS
+    saves = [(i * total + (nsaves - 1) // 2) // (nsaves - 1) for i in range(1, nsaves - 1)]
+    z, crossed = 0, 0
+    for h, ok in steps:
+        if ok:
+            crossed += sum(1 for sp in saves if z < sp < z + h)
+            z += h
+    assert z == total and crossed >= 1
+
+
 def test_gnlse_batch_matches_single_runs():
     from optifax_gb300 import gnlse
     n = 1024
