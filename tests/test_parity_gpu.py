@@ -145,6 +145,16 @@ def test_heun_tight_tolerance(oracle):
     check_parity(oracle, si, E[0], nat.HEUN, nat.VARIANT_BATCH_XTAL)
 
 
+def test_config1_rk23_at_its_own_size(oracle):
+    """Config 1 itself: 2^13 points over 6 ps, 1 mm PPLN (30 um), 1 W sech^2 pump of
+    200 fs, one photon per mode (seed 0), adaptive RK23 at tolerance 1e-6
+    (maxErr 1e-4 %, minErr 5e-6 %), the reference's ODE23 conventions; 10^4 steps."""
+    from optifax_gb300 import _native as nat
+    win, si, E = make_case(N=8192, window=6e-12, length=1e-3, power=1.0, seed=0, error_bounds=(5e-6, 1e-4))
+    info = check_parity(oracle, si, E[0], nat.RK23, nat.VARIANT_ODE23)
+    print(info)
+
+
 def test_mex_batch_shared_schedule(oracle):
     """B = 2 pulses through the 14-argument entry: one schedule for the batch."""
     from optifax_gb300 import solver as sv
