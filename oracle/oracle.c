@@ -86,14 +86,15 @@ static double sample_time(int mode, int i, int n, double dt) {
 
 /* NL = A^2 e^{i phi} + 2 |A|^2 e^{-i phi},  phi = w0 t_i - bdwz
  * (OPO_CUDA_BATCH_XTAL.cu:182-187; NEE_CPU.m:98-101). */
-static void nl_eval(const cplx* A, cplx* NL, int n, const double* tw0, double bdwz) {
+static void nl_eval(const cplx* A, cplx* NL, int n, const cplx* cw0, double bdwz) {
+    const cplx ez = cexpi(-bdwz);                /* exp(i phi) = exp(i w0 t_i) exp(-i bdwz) */
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
     for (int i = 0; i < n; ++i) {
-        cplx e = cexpi(tw0[i] - bdwz);
+        cplx e = cmul(cw0[i], ez);
         cplx a = A[i];
-        double m = cabs2(a);
+        const double m2 = a.re * a.re + a.im * a.im;      /* |A|^2 */
         cplx a2 = cmul(a, a);
-        NL[i] = cadd(cmul(a2, e), cscale(cconj(e), 2.0 * m * m));
+        NL[i] = cadd(cmul(a2, e), cscale(cconj(e), 2.0 * m2));
     }
 }
 
@@ -161,7 +162,9 @@ typedef struct {
     int n;
     fft_plan plan;
     cplx *A0, *A1, *E, *NL, *K1, *K2, *K3, *K4;
-    double* tw0;
+    cplx* cw0;          /* carrier exp(i w0 t_i), tabulated once */
+    cplx* disp;         /* dispersion factor alpha^s exp(-i beta s) for the step size disp_s */
+    double disp_s;
 } work;
 
 static int work_init(work* w, int n, int nb, int time_mode, double w0, double dt) {
@@ -173,17 +176,31 @@ static int work_init(work* w, int n, int nb, int time_mode, double w0, double dt
     w->NL = (cplx*)malloc(sizeof(cplx) * (size_t)n);
     w->K1 = (cplx*)malloc(sz); w->K2 = (cplx*)malloc(sz);
     w->K3 = (cplx*)malloc(sz); w->K4 = (cplx*)malloc(sz);
-    w->tw0 = (double*)malloc(sizeof(double) * (size_t)n);
-    if (!w->A0 || !w->A1 || !w->E || !w->NL || !w->K1 || !w->K2 || !w->K3 || !w->K4 || !w->tw0)
+    w->cw0 = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+    w->disp = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+    w->disp_s = -1.0;
+    if (!w->A0 || !w->A1 || !w->E || !w->NL || !w->K1 || !w->K2 || !w->K3 || !w->K4 || !w->cw0 || !w->disp)
         return -2;
-    for (int i = 0; i < n; ++i) w->tw0[i] = w0 * sample_time(time_mode, i, n, dt);
+    for (int i = 0; i < n; ++i) w->cw0[i] = cexpi(w0 * sample_time(time_mode, i, n, dt));
     return 0;
+}
+
+/* alpha^s exp(-i beta s) per mode (OPO_CUDA_BATCH_XTAL.cu:255-305), recomputed only
+ * when the step size changes */
+static const cplx* disp_factor(work* w, const double* beta, const double* alpha, double s) {
+    if (w->disp_s != s) {
+        const int n = w->n;
+#pragma omp parallel for schedule(static) if (par_ok((size_t)n))
+        for (int i = 0; i < n; ++i) w->disp[i] = cscale(cexpi(-beta[i] * s), pow(alpha[i], s));
+        w->disp_s = s;
+    }
+    return w->disp;
 }
 
 static void work_free(work* w) {
     fft_plan_free(&w->plan);
     free(w->A0); free(w->A1); free(w->E); free(w->NL);
-    free(w->K1); free(w->K2); free(w->K3); free(w->K4); free(w->tw0);
+    free(w->K1); free(w->K2); free(w->K3); free(w->K4); free(w->cw0); free(w->disp);
 }
 
 static double g_at(const sched_ctx* c, int k, int b) {
@@ -201,7 +218,7 @@ static void stage(const sched_ctx* c, work* w, const cplx* X, cplx* K, double po
     double bdwz = p->bdiffw0 * pos * p->h;
     double c_shock = 1.0 / (2.0 * p->dt * p->w0);
     for (int b = 0; b < c->nb; ++b) {
-        nl_eval(X + (size_t)b * n, w->NL, n, w->tw0, bdwz);
+        nl_eval(X + (size_t)b * n, w->NL, n, w->cw0, bdwz);
         k_eval(w->NL, K + (size_t)b * n, n, hmod, g_at(c, kidx, b), c_shock);
     }
 }
@@ -250,11 +267,9 @@ static void dispersion_step(sched_ctx* c, work* w, cplx* E, cplx* A0, int s, int
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
         for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_mex(p->abc_mode, i, n));
         fft_exec(&w->plan, e, 0);
+        const cplx* f = disp_factor(w, c->beta, c->alpha, (double)s);
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
-        for (int i = 0; i < n; ++i) {
-            cplx f = cscale(cexpi(-c->beta[i] * (double)s), pow(c->alpha[i], (double)s));
-            e[i] = cmul(e[i], f);
-        }
+        for (int i = 0; i < n; ++i) e[i] = cmul(e[i], f[i]);
         if (c->Ap) {
             long long off = ((long long)(c->b0 + b) * nchunks + chunk) * (long long)n;
             if (off >= 0 && off + n <= c->ap_len) memcpy(c->Ap + off, e, sizeof(cplx) * (size_t)n);
@@ -462,11 +477,9 @@ static void run_heun_nee(sched_ctx* c, work* w) {
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
                     for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_nee(i, n, p->dt));
                     fft_exec(&w->plan, e, 0);
+                    const cplx* f = disp_factor(w, c->beta, c->alpha, stepmod);
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
-                    for (int i = 0; i < n; ++i) {
-                        cplx f = cscale(cexpi(-c->beta[i] * stepmod), pow(c->alpha[i], stepmod));
-                        e[i] = cmul(e[i], f);
-                    }
+                    for (int i = 0; i < n; ++i) e[i] = cmul(e[i], f[i]);
                     fft_exec(&w->plan, e, 1);
                     cplx* a0 = w->A0 + (size_t)b * n;
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
