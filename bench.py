@@ -804,6 +804,13 @@ def main():
         accuracy["after_trips"] = args.fp64_trips
         accuracy["next_input_rel_l2_after_trips"] = float(np.linalg.norm(e32 - r64["field"]) /
                                                           np.linalg.norm(r64["field"]))
+        # the float-float pass on the same trips: the arithmetic that tracks the FP64
+        # trajectory over many trips (the FP32 one departs once its schedule forks)
+        r2 = ff.fp64_plain_trips(spec, args.fp64_trips, device=local, E0=timed_input, entry="propagate_f32x2")
+        accuracy["f32x2"] = {"trips_per_s": r2["trips_per_s"], "s_per_trip": r2["s_per_trip"],
+                             "speedup_over_fp64": r2["trips_per_s"] / r64["trips_per_s"],
+                             "next_input_rel_l2_after_trips": float(np.linalg.norm(r2["field"] - r64["field"]) /
+                                                                    np.linalg.norm(r64["field"]))}
 
     sweep_line = None
     if rank == 0 and world == 1 and not args.no_sweep:

@@ -465,11 +465,13 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
             "reached_steady_state": flat, "energies": energies, "field": sim.field}
 
 
-def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0=None, trace_cap: int = 0) -> dict:
-    """Round trips through the plain FP64 solver (optifax_propagate_fp64) with the
-    cavity transfer in FP64 on the host.  Timed with CUDA events on the launching
-    stream around all n_trips trips (the host transfer between passes included).
-    Returns seconds per trip, the first pass's crystal output (time domain,
+def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0=None, trace_cap: int = 0,
+                     entry: str = "propagate_fp64") -> dict:
+    """Round trips through the plain FP64 solver (optifax_propagate_fp64; with
+    entry="propagate_f32x2" the float-float pass) with the cavity transfer in FP64 on
+    the host.  Timed with CUDA events on the launching stream around all n_trips
+    trips (the host transfer between passes included).  Returns seconds per trip,
+    the next crystal input, the first pass's crystal output (time domain,
     complex128) and, with trace_cap > 0, its step trace."""
     from . import solver as sv
     a = opo.build_cavity(spec)
@@ -486,9 +488,9 @@ def fp64_plain_trips(spec: opo.CavitySpec, n_trips: int = 2, device: int = 0, E0
     t0 = time.perf_counter()
     ev0.record(stream)
     for i in range(n_trips):
-        A, st, tr = sv.propagate_fp64(torch.from_numpy(E).to(dev), al, be, G, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
-                                      dt=si.dt, n_steps=si.n_steps, max_err=si.max_err, min_err=si.min_err,
-                                      sel=si.sel, trace_cap=trace_cap if i == 0 else 0)
+        A, st, tr = getattr(sv, entry)(torch.from_numpy(E).to(dev), al, be, G, w0=si.w0, bdiffw0=si.bdiffw0,
+                                       h=si.h, dt=si.dt, n_steps=si.n_steps, max_err=si.max_err,
+                                       min_err=si.min_err, sel=si.sel, trace_cap=trace_cap if i == 0 else 0)
         attempts += st["attempts"]
         A = A.cpu().numpy()
         if i == 0:
