@@ -380,7 +380,7 @@ def _to_spec(E: torch.Tensor) -> torch.Tensor:
 def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips: int = 1000,
                      check_every: int = 10, check_tol: float = 0.05, finish_trips: int = 50,
                      flat_tol: float = 1e-3, steady_tol: float = 1e-4, steady_trips: int = 10,
-                     phase_check: bool = True) -> dict:
+                     phase_check: bool = True, check: str = "field") -> dict:
     """max_trips round trips from sim's current state.
 
     Blocks of check_every trips: the first trip of a block is the check (the
@@ -388,7 +388,9 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
     continues from the solver's result); when the relative L2 difference over the
     fed-back band (after the best global signal phase, phase_aligned_err, unless
     phase_check=False) is within check_tol the other trips of the block run on the
-    network, otherwise on the solver.  The last finish_trips trips (and everything
+    network, otherwise on the solver.  check="energy" compares the fed-back band's
+    energy instead (relative error of sum |X|^2 over the band); both errors are
+    recorded for every check either way.  The last finish_trips trips (and everything
     after the network's trips level out to flat_tol) run on the solver, which
     stops early once its steady-state test passes.  net=None runs the solver only.
     """
@@ -401,6 +403,7 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
     energy = torch.zeros(1, dtype=torch.float64, device=dev)
     trips = sur_trips = sol_trips = 0
     checks, energies = [], []
+    check_field, check_energy = [], []
     fallback_blocks = 0
     Y = _to_spec(sim.field) if net is not None else None
     surrogate_until = max_trips - finish_trips if net is not None else 0
@@ -417,9 +420,14 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
         energies.append(float(energy.item()))
         trips += 1
         sol_trips += 1
-        err = phase_aligned_err(Xs, Xt, fbm) if phase_check else \
+        ferr = phase_aligned_err(Xs, Xt, fbm) if phase_check else \
             float(((Xs - Xt)[fbm]).abs().norm() / Xt[fbm].abs().norm().clamp_min(1e-30))
+        et = float((Xt[fbm].abs() ** 2).sum())
+        eerr = abs(float((Xs[fbm].abs() ** 2).sum()) - et) / max(et, 1e-300)
+        err = eerr if check == "energy" else ferr
         checks.append(err)
+        check_field.append(ferr)
+        check_energy.append(eerr)
         n = min(check_every - 1, surrogate_until - trips)
         if n <= 0:
             break
@@ -459,7 +467,8 @@ def run_fast_forward(sim: opo.OpticalSim, net: Optional[FNO], crop, *, max_trips
     flat = len(energies) > steady_trips and bool(np.all(
         np.abs(np.diff(energies[-(steady_trips + 1):])) <= steady_tol * np.abs(energies[-steady_trips:])))
     return {"trips": trips, "surrogate_trips": sur_trips, "solver_trips": sol_trips, "finish_trips": finish,
-            "checks": checks, "fallback_blocks": fallback_blocks, "wall_s": wall,
+            "checks": checks, "check_field_err": check_field, "check_energy_err": check_energy,
+            "check": check, "fallback_blocks": fallback_blocks, "wall_s": wall,
             "trips_per_s": trips / wall if wall > 0 else float("nan"),
             "final_output_signal_energy": energies[-1] if energies else float("nan"),
             "reached_steady_state": flat, "energies": energies, "field": sim.field}

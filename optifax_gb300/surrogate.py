@@ -52,6 +52,22 @@ def init_params(seed: int = 0, spec_scale: float = 1.0) -> np.ndarray:
     return p
 
 
+def pretrained(name: str = "fno_env_spopo"):
+    """(FP32 parameter vector, training record) of a network shipped in
+    optifax_gb300/data: ``fno_env_spopo`` is trained on 20,480 pairs of 5 mm crystal
+    passes of the 2^14-point SPOPO cavity generated by the solver (envelope
+    representation, phase-aligned targets; the record names the command)."""
+    import json
+    import os
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+    params = np.load(os.path.join(here, name + ".npy")).astype(np.float32)
+    with open(os.path.join(here, name + ".json")) as f:
+        meta = json.load(f)
+    if params.size != N_PARAMS:
+        raise ValueError(f"{name}: {params.size} parameters, the network has {N_PARAMS}")
+    return params, meta
+
+
 class FNO:
     """One network on one device: n_bins frequency bins, up to max_batch samples per call."""
 
