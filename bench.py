@@ -679,6 +679,8 @@ def main():
     ap.add_argument("--fp64-trips", type=int, default=2,
                     help="round trips of the plain FP64 solver timed beside the line, from the timed window's "
                          "crystal input (0: skip; also the accuracy record's FP64 side)")
+    ap.add_argument("--surrogate-trips", type=int, default=50,
+                    help="round trips of the surrogate+solver loop measured beside the line (0: skip)")
     ap.add_argument("--no-sweep", action="store_true",
                     help="leave out the uneven-sweep sub-record of the default line")
     ap.add_argument("--fno-case", type=int, default=0,
@@ -812,6 +814,28 @@ def main():
                              "next_input_rel_l2_after_trips": float(np.linalg.norm(r2["field"] - r64["field"]) /
                                                                     np.linalg.norm(r64["field"]))}
 
+    # surrogate + solver (config 5's loop, shortened): the shipped network checked
+    # against the solver every 10 trips from the timed window's end state
+    sur = None
+    if rank == 0 and world == 1 and args.surrogate_trips > 0:
+        from optifax_gb300 import fastforward as ff
+        from optifax_gb300.surrogate import FNO, pretrained
+        params, meta = pretrained()
+        crop = ff.reference_env_crop(spec)
+        net = FNO(n_bins=crop.n_bins, max_batch=1, device=local, params=params)
+        ssim = opo.OpticalSim(spec, device=local)
+        ssim.field = torch.from_numpy(timed_input.astype(np.complex64)).to(dev)
+        fr = ff.run_fast_forward(ssim, net, crop, max_trips=args.surrogate_trips, check_every=10, check_tol=0.05,
+                                 finish_trips=10)
+        sur = {"trips": fr["trips"], "surrogate_trips": fr["surrogate_trips"], "solver_trips": fr["solver_trips"],
+               "trips_per_s": fr["trips_per_s"], "check_tol": 0.05, "check": "fed-back band, phase-aligned field",
+               "check_field_err": fr["check_field_err"], "check_energy_err": fr["check_energy_err"],
+               "network": f"FNO trained on {meta['pairs']} solver pairs; held-out signal error "
+                          f"{meta['training']['val_signal_rel_l2_quantiles'][1]:.2f} vs identity map "
+                          f"{meta['training']['val_identity_rel_l2_median']:.2f}"}
+        if fp64 is not None:
+            sur["speedup_over_fp64"] = fr["trips_per_s"] / fp64["trips_per_s"]
+
     sweep_line = None
     if rank == 0 and world == 1 and not args.no_sweep:
         sweep_line = sweep_record(1, 1, cpu_kw={"n_sample": 8, "fraction": 0.01})
@@ -825,9 +849,9 @@ def main():
             "config": {"workload": WORKLOAD, "n_points": N, "cta_points": M, "cluster": N // M,
                        "parallelism": "replicas" if world > 1 else "single cavity",
                        "solver": "Heun, BATCH_XTAL conventions, errorBounds [2.5e-3, 5e-2] %",
-                       "surrogate": "not used in this measurement (solver-only path): the trained FNO "
-                                    "fails its 5 % solver check on this cavity, so fast-forward falls back "
-                                    "to the solver on every block",
+                       "surrogate": "not used in the value (solver-only path, the one that meets the "
+                                    "accuracy bar per trip); the surrogate+solver loop is measured beside "
+                                    "it in surrogate_solver",
                        "trips_timed": K, "trips_before_timing": W,
                        "attempts_timed": attempts,
                        "l2": "flushed (256 MB write) before the timed launch; the field stays on-chip by design"},
@@ -845,6 +869,7 @@ def main():
             "clocks": clk.summary(),
             "fp64_plain": fp64,
             "accuracy": accuracy,
+            "surrogate_solver": sur,
             "sweep": sweep_line,
         }
         print(json.dumps(line))

@@ -86,3 +86,28 @@ def test_envelope_encode_decode_round_trip():
         idx = (kc + np.arange(lo, hi)) % N
         ref[idx] = Y[0, idx]
     assert np.abs(X - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_trained_surrogate_beats_the_identity_map_on_unseen_trips():
+    """The shipped network (trained on 20,480 solver pairs from cavities with seeds
+    300000 + i) on trips 20..39 of the config-2 cavity itself (seed 1, not in the
+    training set): its phase-aligned signal error is below the identity map's, the
+    prediction "the crystal pass changes nothing" in the interaction picture."""
+    from optifax_gb300 import fastforward as ff, opo
+    from optifax_gb300.surrogate import FNO, pretrained
+    spec = opo.CavitySpec()
+    params, meta = pretrained()
+    crop = ff.reference_env_crop(spec)
+    net = FNO(n_bins=crop.n_bins, max_batch=32, params=params)
+    sim = opo.OpticalSim(spec)
+    r = sim.run(40, history=True)
+    ins = torch.empty_like(r.history)
+    ins[0] = torch.from_numpy(np.fft.fft(sim.arrays.E0).astype(np.complex64)).cuda()
+    ins[1:] = r.history[:-1] * sim.feedback + sim.pump
+    outs = ff.to_interaction(r.history, ff.linear_factor(sim))
+    tgt = ff.align_signal_phase(ins, outs, ff.signal_mask(crop, ins.shape[1], ins.device))
+    X, T = ff.encode_pairs(ins[20:], tgt[20:], crop)
+    err_net = ff.evaluate(net, X, T).cpu().numpy()
+    err_id = ff.signal_rel_err(X[:, :4], T).cpu().numpy()
+    assert np.median(err_net) < np.median(err_id), (np.median(err_net), np.median(err_id))
+    assert np.mean(err_net < err_id) >= 0.6, np.mean(err_net < err_id)
