@@ -205,6 +205,39 @@ def test_uneven_batch_one_call(oracle):
         assert rel_l2(o.cpu().numpy(), ref.A[0]) <= FIELD_TOL
 
 
+def test_config3_instances_at_their_own_sizes():
+    """One instance of every grid size of the config-3 sweep itself (seed 2: the
+    shortest crystal of each size, 0.5-0.8 mm, 2^12..2^16 points), all in one uneven
+    FP32 call, each against the persistent FP64 kernel from the same input: the same
+    step schedule and rel-L2 <= 1e-4, pulse energy <= 1e-6."""
+    import torch
+    from optifax_gb300 import sweep, solver as sv
+    all_insts = sweep.uneven_sweep_instances(256, 2)
+    insts = [all_insts[i] for i in (14, 184, 98, 253, 219)]
+    assert sorted(i.n_points for i in insts) == [4096, 8192, 16384, 32768, 65536]
+    inputs = [sweep.build_inputs(i) for i in insts]
+    specs = sweep.to_specs(inputs, trace_cap=100000)
+    outs, stats = sv.propagate(specs)
+    torch.cuda.synchronize()
+    st = sv.decode_stats(stats)
+    dev = torch.device("cuda:0")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    for (win, si, e), o, spec, s_ in zip(inputs, outs, specs, st):
+        assert s_["status"] == 0
+        tr = spec.trace.cpu().numpy()[:s_["attempts"]]
+        e32 = np.asarray(e).astype(np.complex64).astype(np.complex128)
+        A64, st64, tr64 = sv.propagate_fp64(t(e32), t(si.alpha.astype(np.float64)), t(si.beta.astype(np.float64)),
+                                            t(si.G.astype(np.float64)), w0=si.w0, bdiffw0=si.bdiffw0, h=si.h,
+                                            dt=si.dt, n_steps=si.n_steps, max_err=si.max_err, min_err=si.min_err,
+                                            sel=si.sel, trace_cap=100000)
+        a64 = A64.cpu().numpy()
+        assert np.array_equal(tr[:, :2], tr64[:, :2]), (e.shape, len(tr), len(tr64))
+        assert rel_l2(o.cpu().numpy(), a64) <= FIELD_TOL, rel_l2(o.cpu().numpy(), a64)
+        e_gpu = np.sum(np.abs(o.cpu().numpy().astype(np.complex128)) ** 2)
+        e_ref = np.sum(np.abs(a64) ** 2)
+        assert abs(e_gpu - e_ref) <= ENERGY_TOL * e_ref
+
+
 def test_undepleted_shg_follows_sinc_gpu():
     """The GPU propagator on the undepleted-SHG known answer of tests/test_oracle.py
     (a stronger tone, 0.05, so that the harmonic stands clear of FP32 rounding of the
