@@ -193,6 +193,26 @@ int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_p
                       optifax_pulse_stats* stats, void* stream);
 
 /*
+ * The same batch as optifax_propagate recorded once into a CUDA graph and then
+ * replayed: the graph holds one persistent grid per (cta_points, cluster) group,
+ * forked and joined as optifax_propagate launches them, with its own descriptors
+ * and exchange scratch (no host staging on replay).  The pulses' device pointers
+ * (inputs, outputs, stats) are fixed at capture: every replay reads the inputs'
+ * current contents and rewrites the outputs.  No counterpart in the reference,
+ * whose batch shares one cuFFT plan and one step.  The graph uses the handle's
+ * twiddle tables: destroy it before the handle.  Replays of one graph are ordered
+ * after each other; the caller orders them with other work on its stream.
+ * optifax_graph_kernels returns the number of kernels one replay launches.
+ */
+typedef struct optifax_graph_s* optifax_graph;
+int optifax_propagate_graph(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
+                            int32_t method, int32_t variant, int32_t cta_points,
+                            optifax_pulse_stats* stats, optifax_graph* out);
+int optifax_graph_launch(optifax_graph g, void* stream);
+int optifax_graph_kernels(optifax_graph g);
+int optifax_graph_destroy(optifax_graph g);
+
+/*
  * Run n_cavities independent OPO cavities (e.g. delay scans, replicas) for
  * their round trips in one launch, Heun schedule with the given variant's
  * conventions.  stats (optional, device): per-cavity totals, reserved[0] =

@@ -21,7 +21,8 @@ EXPORTS = ["optifax_create", "optifax_destroy", "optifax_status_string", "optifa
            "optifax_fno_get_params", "optifax_fno_forward", "optifax_fno_backward", "optifax_fno_adam",
            "optifax_ff_encode", "optifax_ff_step",
            "optifax_ff_encode_env", "optifax_ff_decode_env", "optifax_setup_work_bytes", "optifax_setup_pulses",
-           "optifax_gnlse", "optifax_fno_set_grads"]
+           "optifax_gnlse", "optifax_fno_set_grads", "optifax_propagate_graph", "optifax_graph_launch",
+           "optifax_graph_kernels", "optifax_graph_destroy"]
 
 _lib = None
 
@@ -79,6 +80,15 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     lib.optifax_opo_mex_batch.restype = ctypes.c_int
     lib.optifax_propagate.argtypes = [vp, ctypes.POINTER(OptifaxPulse), i32, i32, i32, i32, vp, vp]
     lib.optifax_propagate.restype = ctypes.c_int
+    lib.optifax_propagate_graph.argtypes = [vp, ctypes.POINTER(OptifaxPulse), i32, i32, i32, i32, vp,
+                                            ctypes.POINTER(vp)]
+    lib.optifax_propagate_graph.restype = ctypes.c_int
+    lib.optifax_graph_launch.argtypes = [vp, vp]
+    lib.optifax_graph_launch.restype = ctypes.c_int
+    lib.optifax_graph_kernels.argtypes = [vp]
+    lib.optifax_graph_kernels.restype = ctypes.c_int
+    lib.optifax_graph_destroy.argtypes = [vp]
+    lib.optifax_graph_destroy.restype = ctypes.c_int
     lib.optifax_propagate_noalloc.argtypes = [ctypes.POINTER(OptifaxPulse), i32, vp, vp]
     lib.optifax_propagate_noalloc.restype = ctypes.c_int
     lib.optifax_propagate_fp64.argtypes = [i32, i32, i32, vp, vp, vp, vp, vp, i32, f64, f64, f64, f64,

@@ -205,104 +205,107 @@ int ensure_sync_objects(optifax_context* h, size_t n_streams) {
     return OPTIFAX_OK;
 }
 
-// Stage every group's descriptors (longest work first within a group), then
-// launch one grid per (cta_points, cluster) group.  Groups after the first run
-// on side streams forked from and joined back into `st`, so the block
-// scheduler interleaves them: CTAs of a long group fill SMs as short ones end.
-int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, const VariantCfg& vc,
-                  bool shared, cudaStream_t st) {
-    size_t n_desc = 0, need_xch = 0;
+// Order the groups for launch (longest work first within a group; groups in order
+// of their longest pulse, longest first: the block scheduler serves earlier
+// launches first, so the critical path starts at once and large clusters find
+// whole GPCs free only at the start) and return the exchange scratch they need
+// (complex values).
+size_t order_groups(std::vector<Group>& groups) {
     for (auto& g : groups) {
         std::stable_sort(g.d.begin(), g.d.end(),
                          [](const PulseDev& x, const PulseDev& y) { return pulse_cost(x) > pulse_cost(y); });
     }
-    // groups in order of their longest pulse, longest first: the block scheduler
-    // serves earlier launches first, so the critical path starts at once (and large
-    // clusters find whole GPCs free only at the start)
     auto group_key = [](const Group& g) { return g.d.empty() ? 0.0 : pulse_cost(g.d.front()); };
     std::stable_sort(groups.begin(), groups.end(),
                      [&](const Group& x, const Group& y) { return group_key(x) > group_key(y); });
+    size_t need_xch = 0;
     for (auto& g : groups) {
-        n_desc += g.d.size();
         if (g.C > 1) need_xch += g.d.size() * 2 * (size_t)g.M * g.C;
         for (const auto& d : g.d)
             if (d.fb) need_xch += (size_t)g.M * g.C;    // OPO: the trip's crystal output (cavity scratch)
     }
-    if (need_xch > h->xch_cap) {
-        size_t cap = h->xch_cap * sizeof(float2);
-        int grc = grow_scratch(h, (void**)&h->d_xch, &cap, need_xch * sizeof(float2), st,
-                               "cudaMallocAsync(exchange scratch)");
-        h->xch_cap = cap / sizeof(float2);
-        if (grc) return grc;
-    }
+    return need_xch;
+}
+
+// Descriptors in launch order with their exchange scratch carved from xch.
+std::vector<PulseDev> place_descriptors(std::vector<Group>& groups, float2* xch) {
     std::vector<PulseDev> all;
-    all.reserve(n_desc);
     size_t xoff = 0;
     for (auto& g : groups)
         for (auto& d : g.d) {
-            if (g.C > 1) { d.xch = h->d_xch + xoff; xoff += 2 * (size_t)g.M * g.C; }
-            if (d.fb) { d.xs = h->d_xch + xoff; xoff += (size_t)g.M * g.C; }
+            if (g.C > 1) { d.xch = xch + xoff; xoff += 2 * (size_t)g.M * g.C; }
+            if (d.fb) { d.xs = xch + xoff; xoff += (size_t)g.M * g.C; }
             all.push_back(d);
         }
-    size_t nb = all.size() * sizeof(PulseDev);
-    if (nb > h->desc_cap) {
-        int grc = grow_scratch(h, (void**)&h->d_desc, &h->desc_cap, nb < 4096 ? 4096 : nb * 2, st,
-                               "cudaMallocAsync(descriptors)");
-        if (grc) return grc;
-    }
-    int rc = order_after_previous(h, st);
-    if (rc) return rc;
-    cudaError_t e = cudaMemcpyAsync(h->d_desc, all.data(), nb, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(descriptors)");
-    if (shared) {
-        e = cudaMemsetAsync(h->d_grid_flags, 0, 4 * sizeof(int), st);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync(grid flags)");
-    }
-    rc = ensure_sync_objects(h, groups.size());
-    if (rc) return rc;
-    // tables first: building one synchronises the stream, which must not
-    // happen between the launches
-    std::vector<FftTables> tabv(groups.size());
+    return all;
+}
+
+// The FFT tables of every group, built (once per context) before any launch:
+// building one synchronises the stream, which must not happen between launches.
+int group_tables(optifax_context* h, const std::vector<Group>& groups, cudaStream_t st, std::vector<FftTables>* tabv) {
+    int rc = OPTIFAX_OK;
+    tabv->assign(groups.size(), FftTables{});
     for (size_t gi = 0; gi < groups.size(); ++gi) {
         const int M = groups[gi].M;
         const Twiddle* twp = get_pass_twiddles(h, M, st, &rc);
         if (!twp) return rc;
-        tabv[gi].tw1 = twp;
-        tabv[gi].tw2 = twp + M;
-        tabv[gi].quad = get_table(h, h->quadtw, M, M / 4, st, &rc);       // quarter period of W_M
-        if (!tabv[gi].quad) return rc;
-        tabv[gi].low = get_table(h, h->tw, M * groups[gi].C, 64, st, &rc);  // W_N^i, i < 64
-        if (!tabv[gi].low) return rc;
+        (*tabv)[gi].tw1 = twp;
+        (*tabv)[gi].tw2 = twp + M;
+        (*tabv)[gi].quad = get_table(h, h->quadtw, M, M / 4, st, &rc);       // quarter period of W_M
+        if (!(*tabv)[gi].quad) return rc;
+        (*tabv)[gi].low = get_table(h, h->tw, M * groups[gi].C, 64, st, &rc);  // W_N^i, i < 64
+        if (!(*tabv)[gi].low) return rc;
     }
+    return rc;
+}
+
+// Kernel attributes of every group's kernel (dynamic shared memory, 16-CTA clusters);
+// not stream work, so set before the launches (and outside any capture).
+int group_attributes(optifax_context* h, const std::vector<Group>& groups, int method, const VariantCfg& vc) {
+    for (const auto& g : groups) {
+        const KernelEntry* ke = find_kernel(g.M, g.C, vc.nee ? kHeunNee : method);
+        if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
+                             "no kernel for cta_points=" + std::to_string(g.M) + " cluster=" + std::to_string(g.C));
+        cudaError_t e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ke->smem);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(smem)");
+        if (g.C > 8) {
+            e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(cluster 16)");
+        }
+    }
+    return OPTIFAX_OK;
+}
+
+// One grid per (cta_points, cluster) group; groups after the first run on side
+// streams forked from and joined back into `st`, so the block scheduler
+// interleaves them: CTAs of a long group fill SMs as short ones end.
+int enqueue_groups(optifax_context* h, const std::vector<Group>& groups, int method, const VariantCfg& vc,
+                   bool shared, const PulseDev* d_desc, const std::vector<FftTables>& tabv, int* grid_flags,
+                   cudaStream_t st, const std::vector<cudaStream_t>& side, const std::vector<cudaEvent_t>& ev) {
+    cudaError_t e;
     if (groups.size() > 1) {
-        e = cudaEventRecord(h->ev[0], st);
+        e = cudaEventRecord(ev[0], st);
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaEventRecord");
     }
     size_t off = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
-        Group& g = groups[gi];
+        const Group& g = groups[gi];
         const int M = g.M, C = g.C;
         const KernelEntry* ke = find_kernel(M, C, vc.nee ? kHeunNee : method);
         if (!ke) return fail(h, OPTIFAX_ERR_UNSUPPORTED,
                              "no kernel for cta_points=" + std::to_string(M) + " cluster=" + std::to_string(C));
         const FftTables tabs = tabv[gi];
-        e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ke->smem);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(smem)");
-        if (C > 8) {
-            e = cudaFuncSetAttribute(ke->fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-            if (e != cudaSuccess) return cuda_fail(h, e, "cudaFuncSetAttribute(cluster 16)");
-        }
         KernelCfg cfg;
         cfg.time_mode = vc.time_mode;
         cfg.abc_mode = vc.abc_mode;
         cfg.guard = vc.guard;
         cfg.shared_sched = shared ? 1 : 0;
         cfg.max_attempts_mul = 64;
-        cfg.grid_flags = h->d_grid_flags;
+        cfg.grid_flags = grid_flags;
         cudaStream_t ls = st;
         if (gi > 0) {
-            ls = h->side[gi - 1];
-            e = cudaStreamWaitEvent(ls, h->ev[0], 0);
+            ls = side[gi - 1];
+            e = cudaStreamWaitEvent(ls, ev[0], 0);
             if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamWaitEvent(fork)");
         }
         cudaLaunchConfig_t lc = {};
@@ -322,16 +325,54 @@ int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, co
         }
         lc.attrs = attrs;
         lc.numAttrs = na;
-        const PulseDev* dd = h->d_desc + off;
+        const PulseDev* dd = d_desc + off;
         e = cudaLaunchKernelEx(&lc, ke->fn, dd, tabs, cfg);
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaLaunchKernelEx(pass_kernel)");
         if (gi > 0) {
-            e = cudaEventRecord(h->ev[gi], ls);
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, h->ev[gi], 0);
+            e = cudaEventRecord(ev[gi], ls);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev[gi], 0);
             if (e != cudaSuccess) return cuda_fail(h, e, "join side stream");
         }
         off += g.d.size();
     }
+    return OPTIFAX_OK;
+}
+
+// Stage every group's descriptors into the handle's scratch and launch the groups.
+int launch_groups(optifax_context* h, std::vector<Group>& groups, int method, const VariantCfg& vc,
+                  bool shared, cudaStream_t st) {
+    const size_t need_xch = order_groups(groups);
+    if (need_xch > h->xch_cap) {
+        size_t cap = h->xch_cap * sizeof(float2);
+        int grc = grow_scratch(h, (void**)&h->d_xch, &cap, need_xch * sizeof(float2), st,
+                               "cudaMallocAsync(exchange scratch)");
+        h->xch_cap = cap / sizeof(float2);
+        if (grc) return grc;
+    }
+    std::vector<PulseDev> all = place_descriptors(groups, h->d_xch);
+    size_t nb = all.size() * sizeof(PulseDev);
+    if (nb > h->desc_cap) {
+        int grc = grow_scratch(h, (void**)&h->d_desc, &h->desc_cap, nb < 4096 ? 4096 : nb * 2, st,
+                               "cudaMallocAsync(descriptors)");
+        if (grc) return grc;
+    }
+    int rc = order_after_previous(h, st);
+    if (rc) return rc;
+    cudaError_t e = cudaMemcpyAsync(h->d_desc, all.data(), nb, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync(descriptors)");
+    if (shared) {
+        e = cudaMemsetAsync(h->d_grid_flags, 0, 4 * sizeof(int), st);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync(grid flags)");
+    }
+    rc = ensure_sync_objects(h, groups.size());
+    if (rc) return rc;
+    std::vector<FftTables> tabv;
+    rc = group_tables(h, groups, st, &tabv);
+    if (rc) return rc;
+    rc = group_attributes(h, groups, method, vc);
+    if (rc) return rc;
+    rc = enqueue_groups(h, groups, method, vc, shared, h->d_desc, tabv, h->d_grid_flags, st, h->side, h->ev);
+    if (rc) return rc;
     return mark_done(h, st);
 }
 
@@ -410,27 +451,27 @@ const char* optifax_last_error(optifax_handle h) {
     return h ? h->last_error.c_str() : "null handle";
 }
 
-int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
-                      int32_t method, int32_t variant, int32_t cta_points,
-                      optifax_pulse_stats* stats, void* stream) {
-    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+}  // extern "C"
+
+namespace {
+
+// Validation and grouping by (cta_points, cluster) shared by optifax_propagate and
+// optifax_propagate_graph.
+int propagate_groups(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses, int32_t method,
+                     int32_t variant, int32_t cta_points, optifax_pulse_stats* stats, VariantCfg* vc,
+                     std::vector<Group>* gv) {
     if (!pulses || n_pulses < 1) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "no pulses");
     if (method != OPTIFAX_HEUN && method != OPTIFAX_RK23)
         return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown method");
-    VariantCfg vc;
-    if (!variant_cfg(variant, &vc)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown variant");
-    if (vc.nee && method != OPTIFAX_HEUN)
+    if (!variant_cfg(variant, vc)) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "unknown variant");
+    if (vc->nee && method != OPTIFAX_HEUN)
         return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "the NEE variant is a Heun schedule (NEE_CPU.m)");
     if (cta_points != 0 && (!is_pow2(cta_points) || cta_points < 512 || cta_points > 4096))
         return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "cta_points must be 0 or a power of two in [512, 4096]");
-    cudaError_t e = cudaSetDevice(h->device);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
-    cudaStream_t st = (cudaStream_t)stream;
-    // group pulses by (M, C)
     std::map<std::pair<int, int>, std::vector<PulseDev>> groups;
     for (int i = 0; i < n_pulses; ++i) {
         PulseDev d;
-        int rc = fill_desc(h, pulses[i], vc, &d, stats ? stats + i : nullptr);
+        int rc = fill_desc(h, pulses[i], *vc, &d, stats ? stats + i : nullptr);
         if (rc) return rc;
         int want = pulses[i].cta_points > 0 ? pulses[i].cta_points : cta_points;
         if (want != 0 && (!is_pow2(want) || want < 512 || want > 4096))
@@ -441,10 +482,122 @@ int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_p
         if (C > 16) return fail(h, OPTIFAX_ERR_UNSUPPORTED, "n_points / cta_points exceeds 16");
         groups[{M, C}].push_back(d);
     }
-    std::vector<Group> gv;
-    for (auto& g : groups) gv.push_back(Group{g.first.first, g.first.second, std::move(g.second)});
-    return launch_groups(h, gv, method, vc, false, st);
+    gv->clear();
+    for (auto& g : groups) gv->push_back(Group{g.first.first, g.first.second, std::move(g.second)});
+    return OPTIFAX_OK;
 }
+
+}  // namespace
+
+struct optifax_graph_s {
+    int device = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    PulseDev* d_desc = nullptr;
+    float2* d_xch = nullptr;
+    int kernels = 0;
+};
+
+extern "C" {
+
+int optifax_propagate(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
+                      int32_t method, int32_t variant, int32_t cta_points,
+                      optifax_pulse_stats* stats, void* stream) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    VariantCfg vc;
+    std::vector<Group> gv;
+    int rc = propagate_groups(h, pulses, n_pulses, method, variant, cta_points, stats, &vc, &gv);
+    if (rc) return rc;
+    return launch_groups(h, gv, method, vc, false, (cudaStream_t)stream);
+}
+
+int optifax_graph_destroy(optifax_graph g) {
+    if (!g) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(g->device);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->d_desc) cudaFree(g->d_desc);       // synchronises with any launch still running
+    if (g->d_xch) cudaFree(g->d_xch);
+    delete g;
+    return OPTIFAX_OK;
+}
+
+int optifax_propagate_graph(optifax_handle h, const optifax_pulse* pulses, int32_t n_pulses,
+                            int32_t method, int32_t variant, int32_t cta_points,
+                            optifax_pulse_stats* stats, optifax_graph* out) {
+    if (!h) return OPTIFAX_ERR_NULL_HANDLE;
+    if (!out) return fail(h, OPTIFAX_ERR_INVALID_ARGUMENT, "no output graph");
+    *out = nullptr;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaSetDevice");
+    VariantCfg vc;
+    std::vector<Group> gv;
+    int rc = propagate_groups(h, pulses, n_pulses, method, variant, cta_points, stats, &vc, &gv);
+    if (rc) return rc;
+    optifax_graph g = new (std::nothrow) optifax_graph_s();
+    if (!g) return fail(h, OPTIFAX_ERR_NO_MEMORY, "graph object");
+    g->device = h->device;
+    // the graph owns its descriptors and exchange scratch: later calls on the handle
+    // neither move nor overwrite them
+    const size_t need_xch = order_groups(gv);
+    std::vector<PulseDev> all;
+    cudaStream_t s0 = nullptr;
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> ev;
+    std::vector<FftTables> tabv;
+    auto cleanup = [&](int code) {
+        for (auto s_ : side) cudaStreamDestroy(s_);
+        for (auto e_ : ev) cudaEventDestroy(e_);
+        if (s0) cudaStreamDestroy(s0);
+        if (code) optifax_graph_destroy(g);
+        return code;
+    };
+    if ((e = cudaMalloc(&g->d_xch, (need_xch ? need_xch : 1) * sizeof(float2))) != cudaSuccess)
+        return cleanup(cuda_fail(h, e, "cudaMalloc(graph exchange scratch)"));
+    all = place_descriptors(gv, g->d_xch);
+    if ((e = cudaMalloc(&g->d_desc, all.size() * sizeof(PulseDev))) != cudaSuccess)
+        return cleanup(cuda_fail(h, e, "cudaMalloc(graph descriptors)"));
+    if ((e = cudaMemcpy(g->d_desc, all.data(), all.size() * sizeof(PulseDev), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cleanup(cuda_fail(h, e, "cudaMemcpy(graph descriptors)"));
+    if ((e = cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking)) != cudaSuccess)
+        return cleanup(cuda_fail(h, e, "cudaStreamCreate"));
+    for (size_t i = 0; i < gv.size(); ++i) {
+        cudaStream_t s_;
+        cudaEvent_t e_;
+        if (i + 1 < gv.size()) {
+            if ((e = cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking)) != cudaSuccess)
+                return cleanup(cuda_fail(h, e, "cudaStreamCreate"));
+            side.push_back(s_);
+        }
+        if ((e = cudaEventCreateWithFlags(&e_, cudaEventDisableTiming)) != cudaSuccess)
+            return cleanup(cuda_fail(h, e, "cudaEventCreate"));
+        ev.push_back(e_);
+    }
+    if ((rc = group_tables(h, gv, s0, &tabv))) return cleanup(rc);
+    if ((rc = group_attributes(h, gv, method, vc))) return cleanup(rc);
+    if ((e = cudaStreamSynchronize(s0)) != cudaSuccess) return cleanup(cuda_fail(h, e, "table build"));
+    if ((e = cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cleanup(cuda_fail(h, e, "cudaStreamBeginCapture"));
+    rc = enqueue_groups(h, gv, method, vc, false, g->d_desc, tabv, h->d_grid_flags, s0, side, ev);
+    e = cudaStreamEndCapture(s0, &g->graph);
+    if (rc) return cleanup(rc);
+    if (e != cudaSuccess) return cleanup(cuda_fail(h, e, "cudaStreamEndCapture"));
+    if ((e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
+        return cleanup(cuda_fail(h, e, "cudaGraphInstantiate"));
+    g->kernels = (int)gv.size();
+    *out = g;
+    return cleanup(OPTIFAX_OK);
+}
+
+int optifax_graph_launch(optifax_graph g, void* stream) {
+    if (!g || !g->exec) return OPTIFAX_ERR_INVALID_ARGUMENT;
+    if (cudaSetDevice(g->device) != cudaSuccess) return OPTIFAX_ERR_CUDA;
+    return cudaGraphLaunch(g->exec, (cudaStream_t)stream) == cudaSuccess ? OPTIFAX_OK : OPTIFAX_ERR_CUDA;
+}
+
+int optifax_graph_kernels(optifax_graph g) { return g ? g->kernels : 0; }
 
 int optifax_opo_run(optifax_handle h, const optifax_opo* cavities, int32_t n_cavities,
                     int32_t variant, int32_t cta_points, optifax_pulse_stats* stats, void* stream) {

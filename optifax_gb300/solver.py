@@ -187,6 +187,65 @@ def propagate(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int =
     return [p.out for p in pulses], stats
 
 
+class PropagateGraph:
+    """A batch recorded once by optifax_propagate_graph and replayed by launch():
+    the specs' tensors (inputs read, outputs and stats rewritten on every replay)
+    stay bound to the graph, which keeps references to them."""
+
+    def __init__(self, ctx, handle, outputs, stats, keep, kernels):
+        self.ctx, self.handle, self.outputs, self.stats, self._keep = ctx, handle, outputs, stats, keep
+        self.kernels = kernels
+
+    def launch(self, stream=None):
+        rc = self.ctx.lib.optifax_graph_launch(self.handle, _stream_ptr(stream))
+        check(rc, None, "optifax_graph_launch")
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.optifax_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+def propagate_graph(pulses: Sequence[PulseSpec], *, method: int = HEUN, variant: int = VARIANT_BATCH_XTAL,
+                    cta_points: int = 0) -> PropagateGraph:
+    """Record the batch of ``propagate`` once into a CUDA graph (one persistent grid per
+    cluster shape) and return it; ``graph.launch(stream)`` replays it."""
+    if not pulses:
+        raise ValueError("no pulses")
+    dev = pulses[0].E.device.index or 0
+    ctx = context(dev)
+    arr = (nat.OptifaxPulse * len(pulses))()
+    keep = []
+    for i, p in enumerate(pulses):
+        E = _cuda(p.E, torch.complex64)
+        if p.out is None:
+            p.out = torch.empty_like(E)
+        al, be, G = _cuda(p.alpha, torch.float32), _cuda(p.beta, torch.float32), _cuda(p.G, torch.float32)
+        keep += [E, al, be, G, p.out]
+        d = arr[i]
+        d.n_points, d.n_steps = E.numel(), int(p.n_steps)
+        d.E_in, d.A_out = E.data_ptr(), p.out.data_ptr()
+        d.alpha, d.beta, d.G = al.data_ptr(), be.data_ptr(), G.data_ptr()
+        d.w0, d.h = float(p.w0), float(p.h)
+        d.bdiffw0, d.dt = float(p.bdiffw0), float(p.dt)
+        d.max_err, d.min_err, d.sel = float(p.max_err), float(p.min_err), float(p.sel)
+        d.stepmods_limit = 0
+        d.cta_points = int(p.cta_points or _tuned_cta_points(E.numel(), cta_points))
+    stats = torch.zeros((len(pulses), nat.STATS_BYTES // 4), dtype=torch.int32, device=pulses[0].E.device)
+    torch.cuda.synchronize(pulses[0].E.device)
+    g = ctypes.c_void_p()
+    rc = ctx.lib.optifax_propagate_graph(ctx.handle, arr, len(pulses), int(method), int(variant), int(cta_points),
+                                         stats.data_ptr(), ctypes.byref(g))
+    check(rc, ctx.handle, "optifax_propagate_graph")
+    return PropagateGraph(ctx, g, [p.out for p in pulses], stats, keep, ctx.lib.optifax_graph_kernels(g))
+
+
 def _propagate_wide(entry, E, alpha, beta, G, *, w0, bdiffw0, h, dt, n_steps, max_err, min_err, sel,
                     variant, trace_cap, stream):
     E = _cuda(E, torch.complex128)
