@@ -37,12 +37,18 @@ def main(argv=None):
                     help="keep each target's global signal-phase change (default: remove it, as the check does)")
     ap.add_argument("--weight-decay", type=float, default=0.0)
     ap.add_argument("--power", default="0.5,3.0", help="pump power range of the training cavities [W]")
+    ap.add_argument("--oc-output", type=float, default=0.10, help="output-coupler transmission of the cavities")
+    ap.add_argument("--eval-power", type=float, default=2.0, help="pump power of the evaluation cavity [W]")
+    ap.add_argument("--check", default="field", choices=["field", "energy"])
+    ap.add_argument("--save-params", default="", help="also write the trained parameters here (float16 .npy)")
     args = ap.parse_args(argv)
     from . import fastforward as ff, opo
     from .surrogate import FNO
     os.makedirs(args.out, exist_ok=True)
     summary = {"args": vars(args), "runs": {}}
-    base = opo.CavitySpec(crystal_length=args.crystal_length)
+    base = opo.CavitySpec(crystal_length=args.crystal_length, oc_output=args.oc_output)
+    evalspec = opo.CavitySpec(crystal_length=args.crystal_length, oc_output=args.oc_output,
+                              pump_power=args.eval_power)
     t0 = time.perf_counter()
     pw = tuple(float(x) for x in args.power.split(","))
     specs = ff.training_specs(args.cavities, seed=args.seed, base=base, power=pw)
@@ -66,32 +72,48 @@ def main(argv=None):
               flush=True)
         params = net.params().cpu().numpy()
         np.save(os.path.join(args.out, f"fno_params_{rep}.npy"), params)
+        if args.save_params:
+            np.save(args.save_params, params.astype(np.float16))
         del X, T, net
         torch.cuda.empty_cache()
         if args.eval_trips > 0:
             infer = FNO(n_bins=crop.n_bins, max_batch=1, params=params)
-            fast = ff.run_fast_forward(opo.OpticalSim(base), infer, crop, max_trips=args.eval_trips,
-                                       check_tol=args.check_tol)
-            fast.pop("field")
+            fast = ff.run_fast_forward(opo.OpticalSim(evalspec), infer, crop, max_trips=args.eval_trips,
+                                       check_tol=args.check_tol, check=args.check)
+            summary["_fast_field"] = fast.pop("field")
             fast["energies"] = fast["energies"][-10:]
             run["fast_forward"] = fast
             print(json.dumps({"repr": rep, "fast_forward": {k: fast[k] for k in
                                                             ("trips", "surrogate_trips", "solver_trips",
-                                                             "fallback_blocks", "wall_s", "trips_per_s")},
+                                                             "fallback_blocks", "wall_s", "trips_per_s",
+                                                             "reached_steady_state", "final_output_signal_energy")},
                               "checks": fast["checks"]}), flush=True)
             del infer
         summary["runs"][rep] = run
     if args.solver_only_trips > 0:
-        solo = ff.run_fast_forward(opo.OpticalSim(base), None, ff.reference_crop(base),
+        solo = ff.run_fast_forward(opo.OpticalSim(evalspec), None, ff.reference_crop(base),
                                    max_trips=args.solver_only_trips)
-        solo.pop("field")
+        solo_field = solo.pop("field")
         solo["energies"] = solo["energies"][-10:]
         summary["solver_only"] = solo
+        print(json.dumps({"solver_only": {k: solo[k] for k in ("trips", "wall_s", "trips_per_s", "reached_steady_state",
+                                                               "final_output_signal_energy")}}), flush=True)
+        fast_field = summary.pop("_fast_field", None)
+        if fast_field is not None:
+            # final crystal inputs of the two runs, fed-back band, after the best global signal phase
+            sim = opo.OpticalSim(evalspec)
+            band = sim.feedback.abs() > 0
+            Xa = torch.from_numpy(np.fft.fft(fast_field.cpu().numpy().astype(np.complex128)))
+            Xb = torch.from_numpy(np.fft.fft(solo_field.cpu().numpy().astype(np.complex128)))
+            summary["final_state_fed_back_band_rel_l2"] = ff.phase_aligned_err(Xa, Xb, band.cpu())
+            print(json.dumps({"final_state_fed_back_band_rel_l2": summary["final_state_fed_back_band_rel_l2"]}),
+                  flush=True)
     if args.fp64_trips > 0:
         fp64 = ff.fp64_plain_trips(base, args.fp64_trips)
         fp64.pop("field")
         summary["fp64_plain"] = fp64
         print(json.dumps({"fp64_plain": fp64}), flush=True)
+    summary.pop("_fast_field", None)
     with open(os.path.join(args.out, "train_summary.json"), "w") as f:
         json.dump(summary, f, indent=1, default=float)
 
