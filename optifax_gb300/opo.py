@@ -64,6 +64,7 @@ class CavitySpec:
     error_bounds: tuple = (2.5e-3, 5e-2)
     seed: int = 1
     n_air: float = 1.0
+    step_size: float = 1e-7                  # solver step h [m] (NonlinearCrystal.m:12)
 
 
 @dataclasses.dataclass
@@ -80,7 +81,7 @@ class CavityArrays:
 
 def build_cavity(spec: CavitySpec) -> CavityArrays:
     win = ph.SimWindow(spec.pump_wavelength, spec.n_points, spec.window)
-    xt = ph.Crystal(spec.crystal_length, spec.period, d_eff=spec.d_eff)
+    xt = ph.Crystal(spec.crystal_length, spec.period, d_eff=spec.d_eff, step_size=spec.step_size)
     si = ph.solver_inputs(xt, win, error_bounds=spec.error_bounds)
     n_x = si.n_index                                   # natural FFT order
     r_in = np.sqrt(spec.n_air / n_x)
