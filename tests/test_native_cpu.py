@@ -42,6 +42,11 @@ def test_status_strings_and_null_handle():
     assert lib.optifax_destroy(None) == 5
     assert lib.optifax_propagate(None, None, 0, 0, 0, 0, None, None) == 5
     assert lib.optifax_gnlse(None, None, 0, None) == 5
+    g = ctypes.c_void_p()
+    assert lib.optifax_propagate_graph(None, None, 0, 0, 0, 0, None, ctypes.byref(g)) == 5
+    assert lib.optifax_graph_launch(None, None) == 1
+    assert lib.optifax_graph_destroy(None) == 1
+    assert lib.optifax_graph_kernels(None) == 0
 
 
 def test_create_without_gpu_fails_cleanly():
