@@ -126,11 +126,11 @@ def host_cores() -> int:
 
 
 def oracle_threads(spec, field=None, fraction=0.004):
-    """Threads for the single-cavity CPU baseline: one, or every host core, whichever
-    runs a short sample (the first `fraction` of the pass) faster.  One pass is
-    sequential in z; the oracle spreads its point loops and FFT stages over the
-    threads, which pays only where thread synchronisation is cheap next to a
-    step's work.  Returns (threads, {threads: seconds})."""
+    """Threads for the single-cavity CPU baseline: one, a quarter, half or all of the
+    host cores, whichever runs a short sample (the first `fraction` of the pass)
+    fastest.  One pass is sequential in z; the oracle runs it as one parallel
+    region, each thread on its own span of points (a power of two of them), with
+    a barrier per attempt and a few per FFT.  Returns (threads, {threads: seconds})."""
     import numpy as np
     from oracle import oracle as orc
     from optifax_gb300.opo import build_cavity
@@ -139,7 +139,8 @@ def oracle_threads(spec, field=None, fraction=0.004):
     S = max(8, int(si.n_steps * fraction))
     E = arr.E0 if field is None else field
     times = {}
-    for nt in sorted({1, host_cores()}):
+    cores = host_cores()
+    for nt in sorted({1, max(1, cores // 4), max(1, cores // 2), cores}):
         t0 = time.perf_counter()
         orc.run(E, si.alpha, si.G[:S], si.beta, w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=S,
                 dt=si.dt, max_err=si.max_err, min_err=si.min_err, sel=float(np.ceil(S / 4)), nthreads=nt)

@@ -38,11 +38,16 @@
  * available here); any transform exact to FP64 rounding is equivalent.
  *
  * Threads: independent schedules (pulses) run in parallel.  A call with one
- * schedule of 4096 points or more and an explicit thread count (nthreads > 0)
- * spreads the pass's point loops and FFT butterflies over those threads
- * instead; with nthreads = 0 a pass stays on one thread.  Each point's
- * arithmetic is the same whichever thread does it and the only reductions (a
- * max and an OR) are exact, so the results do not depend on the thread count.
+ * schedule of 4096 points or more and an explicit thread count (nthreads > 1)
+ * spreads the pass over those threads instead; with nthreads = 0 a pass stays
+ * on one thread.  The Heun MEX schedule of one pulse runs as one parallel
+ * region per pass (run_heun_mex_team): each thread owns a span of points, updates
+ * both stages of its span with a two-point halo, and runs the FFT stages that fit
+ * its span without synchronisation, so a rejected attempt costs one barrier and
+ * an accepted one 2 log2(T) + 4.  The other schedules spread each point loop and
+ * FFT stage separately.  Each point's arithmetic is the same whichever thread
+ * does it and the only reductions (a max and an OR) are exact, so the results do
+ * not depend on the thread count.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -86,32 +91,37 @@ static double sample_time(int mode, int i, int n, double dt) {
 
 /* NL = A^2 e^{i phi} + 2 |A|^2 e^{-i phi},  phi = w0 t_i - bdwz
  * (OPO_CUDA_BATCH_XTAL.cu:182-187; NEE_CPU.m:98-101). */
+static inline cplx nl_point(cplx a, cplx cw, cplx ez) {
+    cplx e = cmul(cw, ez);
+    const double m2 = a.re * a.re + a.im * a.im;          /* |A|^2 */
+    cplx a2 = cmul(a, a);
+    return cadd(cmul(a2, e), cscale(cconj(e), 2.0 * m2));
+}
+
 static void nl_eval(const cplx* A, cplx* NL, int n, const cplx* cw0, double bdwz) {
     const cplx ez = cexpi(-bdwz);                /* exp(i phi) = exp(i w0 t_i) exp(-i bdwz) */
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
-    for (int i = 0; i < n; ++i) {
-        cplx e = cmul(cw0[i], ez);
-        cplx a = A[i];
-        const double m2 = a.re * a.re + a.im * a.im;      /* |A|^2 */
-        cplx a2 = cmul(a, a);
-        NL[i] = cadd(cmul(a2, e), cscale(cconj(e), 2.0 * m2));
-    }
+    for (int i = 0; i < n; ++i) NL[i] = nl_point(A[i], cw0[i], ez);
 }
 
 /* K = -i h G (NL - i/(2 dt w0) (NL[i+1] - NL[i-1])), periodic neighbours
  * (OPO_CUDA_BATCH_XTAL.cu:221-249; NEE_CPU.m:103-105). */
+static inline cplx k_point(cplx nlp, cplx nlm, cplx nl, double hmod, double g, double c_shock) {
+    cplx d = csub(nlp, nlm);
+    /* i * c_shock * d */
+    cplx id = cmk(-c_shock * d.im, c_shock * d.re);
+    cplx in = csub(nl, id);
+    /* -i * hG * in */
+    double hg = hmod * g;
+    return cmk(hg * in.im, -hg * in.re);
+}
+
 static void k_eval(const cplx* NL, cplx* K, int n, double hmod, double g, double c_shock) {
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
     for (int i = 0; i < n; ++i) {
         int ip = (i + 1 == n) ? 0 : i + 1;
         int im = (i == 0) ? n - 1 : i - 1;
-        cplx d = csub(NL[ip], NL[im]);
-        /* i * c_shock * d */
-        cplx id = cmk(-c_shock * d.im, c_shock * d.re);
-        cplx in = csub(NL[i], id);
-        /* -i * hG * in */
-        double hg = hmod * g;
-        K[i] = cmk(hg * in.im, -hg * in.re);
+        K[i] = k_point(NL[ip], NL[im], NL[i], hmod, g, c_shock);
     }
 }
 
@@ -158,16 +168,24 @@ typedef struct {
     ofx_oracle_stats* stats;
 } sched_ctx;
 
+#define OFX_DISP_SLOTS 8
+
 typedef struct {
     int n;
     fft_plan plan;
     cplx *A0, *A1, *E, *NL, *K1, *K2, *K3, *K4;
     cplx* cw0;          /* carrier exp(i w0 t_i), tabulated once */
-    cplx* disp;         /* dispersion factor alpha^s exp(-i beta s) for the step size disp_s */
-    double disp_s;
+    double* abc;        /* absorber factor per point, tabulated once */
+    cplx* disp;         /* OFX_DISP_SLOTS tables of alpha^s exp(-i beta s); slot disp_slot(s) */
+    double disp_s[OFX_DISP_SLOTS];      /* the step size each slot holds, -1 for none */
 } work;
 
-static int work_init(work* w, int n, int nb, int time_mode, double w0, double dt) {
+/* Step sizes are whole numbers of z-samples; a pass moves among a few of them, so
+ * a small direct-mapped cache of dispersion tables (keyed by s mod 8) saves the
+ * n exponentials and powers of a table rebuild at most changes of step size. */
+static int disp_slot(double s) { return (int)((long long)s & (OFX_DISP_SLOTS - 1)); }
+
+static int work_init(work* w, int n, int nb, int time_mode, int nee, int abc_mode, double w0, double dt) {
     memset(w, 0, sizeof(*w));
     w->n = n;
     if (fft_plan_init(&w->plan, n)) return -1;
@@ -177,30 +195,37 @@ static int work_init(work* w, int n, int nb, int time_mode, double w0, double dt
     w->K1 = (cplx*)malloc(sz); w->K2 = (cplx*)malloc(sz);
     w->K3 = (cplx*)malloc(sz); w->K4 = (cplx*)malloc(sz);
     w->cw0 = (cplx*)malloc(sizeof(cplx) * (size_t)n);
-    w->disp = (cplx*)malloc(sizeof(cplx) * (size_t)n);
-    w->disp_s = -1.0;
-    if (!w->A0 || !w->A1 || !w->E || !w->NL || !w->K1 || !w->K2 || !w->K3 || !w->K4 || !w->cw0 || !w->disp)
+    w->abc = (double*)malloc(sizeof(double) * (size_t)n);
+    w->disp = (cplx*)malloc(sizeof(cplx) * (size_t)n * OFX_DISP_SLOTS);
+    for (int j = 0; j < OFX_DISP_SLOTS; ++j) w->disp_s[j] = -1.0;
+    if (!w->A0 || !w->A1 || !w->E || !w->NL || !w->K1 || !w->K2 || !w->K3 || !w->K4 || !w->cw0 || !w->abc ||
+        !w->disp)
         return -2;
-    for (int i = 0; i < n; ++i) w->cw0[i] = cexpi(w0 * sample_time(time_mode, i, n, dt));
+    for (int i = 0; i < n; ++i) {
+        w->cw0[i] = cexpi(w0 * sample_time(time_mode, i, n, dt));
+        w->abc[i] = nee ? abc_factor_nee(i, n, dt) : abc_factor_mex(abc_mode, i, n);
+    }
     return 0;
 }
 
 /* alpha^s exp(-i beta s) per mode (OPO_CUDA_BATCH_XTAL.cu:255-305), recomputed only
  * when the step size changes */
 static const cplx* disp_factor(work* w, const double* beta, const double* alpha, double s) {
-    if (w->disp_s != s) {
+    const int slot = disp_slot(s);
+    cplx* f = w->disp + (size_t)slot * (size_t)w->n;
+    if (w->disp_s[slot] != s) {
         const int n = w->n;
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
-        for (int i = 0; i < n; ++i) w->disp[i] = cscale(cexpi(-beta[i] * s), pow(alpha[i], s));
-        w->disp_s = s;
+        for (int i = 0; i < n; ++i) f[i] = cscale(cexpi(-beta[i] * s), pow(alpha[i], s));
+        w->disp_s[slot] = s;
     }
-    return w->disp;
+    return f;
 }
 
 static void work_free(work* w) {
     fft_plan_free(&w->plan);
     free(w->A0); free(w->A1); free(w->E); free(w->NL);
-    free(w->K1); free(w->K2); free(w->K3); free(w->K4); free(w->cw0); free(w->disp);
+    free(w->K1); free(w->K2); free(w->K3); free(w->K4); free(w->cw0); free(w->abc); free(w->disp);
 }
 
 static double g_at(const sched_ctx* c, int k, int b) {
@@ -227,22 +252,26 @@ static void stage(const sched_ctx* c, work* w, const cplx* X, cplx* K, double po
  * OPO_CUDA_BATCH_XTAL.cu:325-349 (pct = 100 |E-A1|/(|E|+1), >= maxErr sets
  * flag0, else >= minErr sets flag1, points with |E| == 0 skipped);
  * ODE23 uses 4*100*0.5*|E-A1| (OPO_CUDA_ODE23.cu:332-335). */
+static inline int classify_point(const ofx_oracle_params* p, cplx e, cplx a1, double scale, double* pm) {
+    int flags = 0;
+    double ae = cabs2(e);
+    if (ae > 0) {
+        double pct = scale * cabs2(csub(e, a1)) / (ae + 1.0);
+        if (pct > *pm) *pm = pct;
+        if (pct >= p->maxErr) flags |= 1;
+        else if (pct >= p->minErr) flags |= 2;
+    }
+    if (isnan(e.re) || isnan(e.im)) flags |= 4;
+    return flags;
+}
+
 static int classify(const sched_ctx* c, const cplx* E, const cplx* A1, double scale,
                     double* pct_max_out) {
     const ofx_oracle_params* p = c->p;
     int flags = 0; double pm = 0.0;
     size_t tot = (size_t)p->N * (size_t)c->nb;
 #pragma omp parallel for schedule(static) reduction(max : pm) reduction(| : flags) if (par_ok(tot))
-    for (size_t i = 0; i < tot; ++i) {
-        double ae = cabs2(E[i]);
-        if (ae > 0) {
-            double pct = scale * cabs2(csub(E[i], A1[i])) / (ae + 1.0);
-            if (pct > pm) pm = pct;
-            if (pct >= p->maxErr) flags |= 1;
-            else if (pct >= p->minErr) flags |= 2;
-        }
-        if (isnan(E[i].re) || isnan(E[i].im)) flags |= 4;
-    }
+    for (size_t i = 0; i < tot; ++i) flags |= classify_point(p, E[i], A1[i], scale, &pm);
     *pct_max_out = pm;
     return flags;
 }
@@ -265,7 +294,7 @@ static void dispersion_step(sched_ctx* c, work* w, cplx* E, cplx* A0, int s, int
     for (int b = 0; b < c->nb; ++b) {
         cplx* e = E + (size_t)b * n;
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
-        for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_mex(p->abc_mode, i, n));
+        for (int i = 0; i < n; ++i) e[i] = cscale(e[i], w->abc[i]);
         fft_exec(&w->plan, e, 0);
         const cplx* f = disp_factor(w, c->beta, c->alpha, (double)s);
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
@@ -347,6 +376,169 @@ static void run_heun_mex(sched_ctx* c, work* w) {
     c->stats->nchunks = nchunks;
     if (c->n_attempts) *c->n_attempts = attempt;
 }
+
+#ifdef _OPENMP
+/* Team size for one pass: the largest power of two within the thread count that
+ * leaves each thread at least 1024 points; 1 (the loop-by-loop path) for a lone
+ * thread, a batch sharing one schedule, or a call already inside a parallel region. */
+static int team_size(int n, int nb) {
+    if (!t_inner || nb != 1 || n < OFX_PAR_MIN || omp_in_parallel()) return 1;
+    int t = 1, m = omp_get_max_threads();
+    while (2 * t <= m && n / (2 * t) >= 1024) t *= 2;
+    return t;
+}
+
+/* Both Heun stages and the error test for points [lo, hi) of one pulse.  The
+ * centred difference in K needs NL one point further out on each side, and the
+ * second stage needs A1 (hence K1) one point further out again, so the span
+ * recomputes NL1 on [lo-2, hi+2) and K1, A1, NL2 on [lo-1, hi+1) (indices
+ * periodic).  Every value is the expression run_heun_mex evaluates for that
+ * point.  Scratch: 4 (hi - lo + 4) values.  Returns the classify flags; *pm the
+ * largest percentage. */
+static int heun_span(const ofx_oracle_params* p, const cplx* A0, cplx* E, const cplx* cw0, int lo, int hi,
+                     cplx ez1, cplx ez2, double hmod, double g, double c_shock, cplx* scratch, double* pm) {
+    const int n = p->N, m = hi - lo + 4;
+    cplx *nl1 = scratch, *k1 = scratch + m, *a1 = scratch + 2 * m, *nl2 = scratch + 3 * m;
+#define OFX_WRAP(i) ((i) < 0 ? (i) + n : ((i) >= n ? (i) - n : (i)))
+    for (int l = 0; l < m; ++l) {                       /* point lo - 2 + l */
+        const int gi = OFX_WRAP(lo - 2 + l);
+        nl1[l] = nl_point(A0[gi], cw0[gi], ez1);
+    }
+    for (int l = 1; l < m - 1; ++l) {
+        const int gi = OFX_WRAP(lo - 2 + l);
+        k1[l] = k_point(nl1[l + 1], nl1[l - 1], nl1[l], hmod, g, c_shock);
+        a1[l] = cadd(A0[gi], cadd(cscale(k1[l], 0.5), cscale(k1[l], 0.5)));
+        nl2[l] = nl_point(a1[l], cw0[gi], ez2);
+    }
+#undef OFX_WRAP
+    int flags = 0;
+    for (int l = 2; l < m - 2; ++l) {
+        const int i = lo - 2 + l;
+        cplx k2 = k_point(nl2[l + 1], nl2[l - 1], nl2[l], hmod, g, c_shock);
+        E[i] = cadd(A0[i], cadd(cscale(k2, 0.5), cscale(k1[l], 0.5)));
+        flags |= classify_point(p, E[i], a1[l], 100.0, pm);
+    }
+    return flags;
+}
+
+/* run_heun_mex for one pulse on a team of T threads (one parallel region for the
+ * whole pass).  Every thread runs the step control on its own copy of the
+ * schedule state; the flags and the largest percentage are combined exactly (OR,
+ * max) so every copy takes the same decisions.  Thread 0 alone writes the
+ * statistics, trace and stepmods.  Per attempt: the span update, one barrier for
+ * the error test; per accepted step: absorber, FFT, dispersion, snapshot, inverse
+ * FFT and 1/N on each thread's own points, with barriers only where a step reads
+ * other threads' points.  The results are bit-identical to run_heun_mex.
+ * Returns 0, or -1 (nothing done) when the team or its scratch is unavailable. */
+static int run_heun_mex_team(sched_ctx* c, work* w, int T) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N, span = n / T;
+    const double sel = p->sel, inv_n = 1.0 / (double)n, c_shock = 1.0 / (2.0 * p->dt * p->w0);
+    int nchunks = (int)((double)p->S / sel);
+    if (p->chunk_mode == OFX_CHUNKS_CEIL && (double)nchunks * sel < (double)p->S) nchunks += 1;
+    cplx* scratch = (cplx*)malloc(sizeof(cplx) * 4 * (size_t)(span + 4) * (size_t)T);
+    double* part_pm = (double*)malloc(sizeof(double) * 2 * (size_t)T);
+    int* part_fl = (int*)malloc(sizeof(int) * 2 * (size_t)T);
+    int ran = 0;
+    if (scratch && part_pm && part_fl) {
+#pragma omp parallel num_threads(T)
+        if (omp_get_num_threads() == T) {
+            const int tid = omp_get_thread_num(), lo = tid * span, hi = lo + span;
+            cplx* mine = scratch + 4 * (size_t)(span + 4) * (size_t)tid;
+            double k = 0.0, stepprev = 4.0, stepmod = stepprev, stepend, pm = 0.0;
+            double my_s[OFX_DISP_SLOTS];        /* this thread's view of the table slots (its own points) */
+            for (int j = 0; j < OFX_DISP_SLOTS; ++j) my_s[j] = -1.0;
+            int attempt = 0;
+            for (int chunk = 0; chunk < nchunks; ++chunk) {
+                stepmod = stepprev;
+                double cend = (double)(chunk + 1) * sel;
+                for (; k < cend && (p->chunk_mode != OFX_CHUNKS_CEIL || k < (double)p->S); k = k + stepmod) {
+                    const int kidx = (int)k;
+                    const double hmod = stepmod * p->h, g = g_at(c, kidx, 0);
+                    const cplx ez1 = cexpi(-(p->bdiffw0 * k * p->h));
+                    const cplx ez2 = cexpi(-(p->bdiffw0 * (k + stepmod) * p->h));
+                    double my_pm = 0.0;
+                    const int slot = attempt & 1;
+                    part_fl[slot * T + tid] = heun_span(p, w->A0, w->E, w->cw0, lo, hi, ez1, ez2, hmod, g,
+                                                        c_shock, mine, &my_pm);
+                    part_pm[slot * T + tid] = my_pm;
+#pragma omp barrier
+                    int fl = 0;
+                    pm = 0.0;
+                    for (int t = 0; t < T; ++t) {
+                        fl |= part_fl[slot * T + t];
+                        if (part_pm[slot * T + t] > pm) pm = part_pm[slot * T + t];
+                    }
+                    fl = get_flags(c, attempt, fl);
+                    if (tid == 0) {
+                        if (fl & 4) c->stats->status |= OFX_ORACLE_STATUS_NAN;
+                        c->stats->pct_max_last = pm;
+                    }
+                    if ((fl & 1) && stepmod > 1.0 && (k - stepmod) > 0.0) {
+                        if (tid == 0) { record(c, attempt, kidx, (int)stepmod, fl, 0); c->stats->rejected++; }
+                        k = k - stepmod;
+                        stepmod = stepmod - 1.0;
+                        stepprev = stepmod;
+                    } else {
+                        const int s = (int)stepmod;
+                        if (tid == 0) {
+                            record(c, attempt, kidx, s, fl, 1);
+                            c->stats->accepted++;
+                            c->stats->z_steps += (long long)stepmod;
+                        }
+                        /* dispersion_step on this thread's points: the absorber is
+                         * applied in the bit-reversal gather into K1 (free in this
+                         * path), the dispersion factor in the gather back into E */
+                        const int slot = disp_slot((double)s);
+                        cplx* f = w->disp + (size_t)slot * (size_t)n;
+                        if (my_s[slot] != (double)s) {
+                            for (int i = lo; i < hi; ++i)
+                                f[i] = cscale(cexpi(-c->beta[i] * (double)s), pow(c->alpha[i], (double)s));
+                            my_s[slot] = (double)s;
+                        }
+                        const int* rev = w->plan.rev;
+                        cplx *e = w->E, *y = w->K1;
+                        for (int i = lo; i < hi; ++i) y[i] = cscale(e[rev[i]], w->abc[rev[i]]);
+                        fft_team_stages(&w->plan, y, 0, tid, T);
+                        if (c->Ap) {
+                            long long off = ((long long)c->b0 * nchunks + chunk) * (long long)n;
+                            if (off >= 0 && off + n <= c->ap_len) {
+                                for (int i = lo; i < hi; ++i) c->Ap[off + i] = cmul(y[i], f[i]);
+                            } else if (tid == 0) c->stats->status |= OFX_ORACLE_STATUS_AP_RANGE;
+                        }
+                        for (int i = lo; i < hi; ++i) e[i] = cmul(y[rev[i]], f[rev[i]]);
+                        fft_team_stages(&w->plan, e, 1, tid, T);
+                        for (int i = lo; i < hi; ++i) w->A0[i] = cscale(e[i], inv_n);
+                        if (tid == 0 && c->stepmods && kidx < p->stepmods_limit && kidx < p->S && kidx >= 0)
+                            c->stepmods[kidx] = (double)s;
+#pragma omp barrier
+                        if (k + stepmod >= cend && k < cend - 1.0) {
+                            stepend = (cend - k) - 1.0;
+                            stepprev = stepmod;
+                            stepmod = stepend;
+                        } else {
+                            if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.0) < cend - 1.0)
+                                stepmod = stepmod + 1.0;
+                            stepprev = stepmod;
+                        }
+                    }
+                    attempt++;
+                }
+            }
+            if (tid == 0) {
+                c->stats->attempts = attempt;
+                c->stats->k_final = k;
+                c->stats->stepmod_final = stepmod;
+                c->stats->nchunks = nchunks;
+                if (c->n_attempts) *c->n_attempts = attempt;
+                ran = 1;
+            }
+        }
+    }
+    free(scratch); free(part_pm); free(part_fl);
+    return ran ? 0 : -1;
+}
+#endif
 
 /* OPO_CUDA_ODE23.cu:375-557 */
 static void run_rk23_mex(sched_ctx* c, work* w) {
@@ -475,7 +667,7 @@ static void run_heun_nee(sched_ctx* c, work* w) {
                 for (int b = 0; b < c->nb; ++b) {
                     cplx* e = w->E + (size_t)b * n;
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
-                    for (int i = 0; i < n; ++i) e[i] = cscale(e[i], abc_factor_nee(i, n, p->dt));
+                    for (int i = 0; i < n; ++i) e[i] = cscale(e[i], w->abc[i]);
                     fft_exec(&w->plan, e, 0);
                     const cplx* f = disp_factor(w, c->beta, c->alpha, stepmod);
 #pragma omp parallel for schedule(static) if (par_ok((size_t)n))
@@ -513,11 +705,20 @@ static int run_schedule(sched_ctx* c) {
     const ofx_oracle_params* p = c->p;
     work w;
     int time_mode = p->method == OFX_ORACLE_HEUN_NEE ? OFX_TIME_NEE : p->time_mode;
-    if (work_init(&w, p->N, c->nb, time_mode, p->w0, p->dt)) { work_free(&w); return OFX_ORACLE_ENOMEM; }
+    if (work_init(&w, p->N, c->nb, time_mode, p->method == OFX_ORACLE_HEUN_NEE, p->abc_mode, p->w0, p->dt)) {
+        work_free(&w);
+        return OFX_ORACLE_ENOMEM;
+    }
     memcpy(w.A0, c->E_in + (size_t)c->b0 * p->N, sizeof(cplx) * (size_t)p->N * c->nb);
     memset(c->stats, 0, sizeof(*c->stats));
-    if (p->method == OFX_ORACLE_HEUN_MEX) run_heun_mex(c, &w);
-    else if (p->method == OFX_ORACLE_RK23_MEX) run_rk23_mex(c, &w);
+    if (p->method == OFX_ORACLE_HEUN_MEX) {
+#ifdef _OPENMP
+        int T = team_size(p->N, c->nb);
+        if (T < 2 || run_heun_mex_team(c, &w, T) != 0) run_heun_mex(c, &w);
+#else
+        run_heun_mex(c, &w);
+#endif
+    } else if (p->method == OFX_ORACLE_RK23_MEX) run_rk23_mex(c, &w);
     else run_heun_nee(c, &w);
     memcpy(c->A_out + (size_t)c->b0 * p->N, w.A0, sizeof(cplx) * (size_t)p->N * c->nb);
     work_free(&w);

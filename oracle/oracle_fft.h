@@ -129,4 +129,53 @@ static void fft_exec(const fft_plan* p, cplx* x, int inverse) {
     }
 }
 
+#ifdef _OPENMP
+/* The butterfly stages of fft_exec spread over a team of T threads (T a power of
+ * two, n / T at least 2), called by every thread of an enclosing parallel region
+ * with its own tid.  Thread tid owns points [tid n/T, (tid+1) n/T) and must itself
+ * have written its own points of x in bit-reversed order (a gather
+ * x[i] = src[rev[i]], which reads only and keeps each thread's writes in its own
+ * cache lines).  Stages whose blocks fit in one thread's span run without
+ * synchronisation; a barrier, then the last log2 T stages split their butterflies
+ * evenly, each followed by a barrier.  Each element sees the same butterflies,
+ * with the same twiddles, as in fft_exec, so the result is bit-identical.  On
+ * return x is complete. */
+static void fft_team_stages(const fft_plan* p, cplx* x, int inverse, int tid, int T) {
+    const int n = p->n, span = n / T, lo = tid * span, hi = lo + span;
+    const cplx* tw = p->tws;
+    int len = 2;
+    for (; len <= span; len <<= 1) {
+        const int half = len >> 1;
+        for (int b = lo; b < hi; b += len) {
+            cplx* xa = x + b;
+            cplx* xb = x + b + half;
+            for (int j = 0; j < half; ++j) {
+                cplx w = tw[j];
+                if (inverse) w = cconj(w);
+                cplx u = xa[j], v = cmul(xb[j], w);
+                xa[j] = cadd(u, v);
+                xb[j] = csub(u, v);
+            }
+        }
+        tw += half;
+    }
+#pragma omp barrier
+    const int q0 = tid * (n / 2 / T), q1 = q0 + n / 2 / T;
+    for (; len <= n; len <<= 1) {
+        const int half = len >> 1;
+        for (int q = q0; q < q1; ++q) {
+            const int j = q & (half - 1);
+            const int b = (q - j) << 1;
+            cplx w = tw[j];
+            if (inverse) w = cconj(w);
+            cplx u = x[b + j], v = cmul(x[b + j + half], w);
+            x[b + j] = cadd(u, v);
+            x[b + j + half] = csub(u, v);
+        }
+        tw += half;
+#pragma omp barrier
+    }
+}
+#endif
+
 #endif
