@@ -840,8 +840,9 @@ def main():
                                              check_tol=0.05, finish_trips=10, check="energy")
         fr, fo = runs["surrogate"], runs["solver"]
         e_s, e_o = np.array(fr["energies"]), np.array(fo["energies"])
-        fbm = s_.feedback.abs() > 0
-        final = ff.phase_aligned_err(torch.fft.fft(fr["field"]), torch.fft.fft(fo["field"]), fbm)
+        fbm = np.abs(s_.feedback.cpu().numpy()) > 0
+        final = ff.phase_aligned_err(np.fft.fft(fr["field"].cpu().numpy()), np.fft.fft(fo["field"].cpu().numpy()),
+                                     fbm)
         sur = {"trips": fr["trips"], "surrogate_trips": fr["surrogate_trips"], "solver_trips": fr["solver_trips"],
                "trips_per_s": fr["trips_per_s"], "check_tol": 0.05,
                "check": "fed-back band energy (relative error of its sum |X|^2, network trip vs solver trip from "
