@@ -92,7 +92,9 @@ def test_trained_surrogate_beats_the_identity_map_on_unseen_trips():
     """The shipped network (trained on 20,480 solver pairs from cavities with seeds
     300000 + i) on trips 20..39 of the config-2 cavity itself (seed 1, not in the
     training set): its phase-aligned signal error is below the identity map's, the
-    prediction "the crystal pass changes nothing" in the interaction picture."""
+    prediction "the crystal pass changes nothing" in the interaction picture, and so
+    is its error in the fed-back band's energy, which the fast-forward loop's energy
+    check compares; on some of these trips that check (5 %) passes."""
     from optifax_gb300 import fastforward as ff, opo
     from optifax_gb300.surrogate import FNO, pretrained
     spec = opo.CavitySpec()
@@ -111,3 +113,20 @@ def test_trained_surrogate_beats_the_identity_map_on_unseen_trips():
     err_id = ff.signal_rel_err(X[:, :4], T).cpu().numpy()
     assert np.median(err_net) < np.median(err_id), (np.median(err_net), np.median(err_id))
     assert np.mean(err_net < err_id) >= 0.6, np.mean(err_net < err_id)
+    # the fast-forward loop's energy check on the same trips: relative error of the
+    # fed-back band's energy, the network's predicted crystal output against the
+    # solver's, beside the identity map's (linear propagation only)
+    D = ff.linear_factor(sim)
+    fbm = np.abs(sim.feedback.cpu().numpy()) > 0
+    e_net, e_id = [], []
+    for t in range(20, 40):
+        x, sig = ff.encode(ins[t:t + 1], crop)
+        Xs = torch.empty(crop.n_points, dtype=torch.complex64, device=ins.device)
+        ff.step(crop, sim.feedback, sim.pump, None, y=net.forward(x), sigma=sig, lin=D, X_out=Xs)
+        et = np.sum(np.abs(r.history[t].cpu().numpy().astype(np.complex128)[fbm]) ** 2)
+        for pred, out in ((Xs, e_net), (ins[t] * D, e_id)):
+            out.append(abs(np.sum(np.abs(pred.cpu().numpy().astype(np.complex128)[fbm]) ** 2) - et) / et)
+    e_net, e_id = np.array(e_net), np.array(e_id)
+    assert np.median(e_net) < np.median(e_id), (np.median(e_net), np.median(e_id))
+    assert np.sum(e_net <= 0.05) >= 2, e_net          # trips on which a 5 % energy check passes
+    assert np.mean(e_net < e_id) >= 0.6, np.mean(e_net < e_id)
