@@ -19,8 +19,8 @@ namespace {
 
 const std::vector<XKernel<ff>>& ff_kernels() {
     static const std::vector<XKernel<ff>> v = {
-        xkernel<ff, 512, 1, false>(),   xkernel<ff, 1024, 1, false>(),  xkernel<ff, 1024, 2, false>(),
-        xkernel<ff, 1024, 4, false>(),  xkernel<ff, 1024, 8, false>(),  xkernel<ff, 1024, 16, false>(),
+        xkernel<ff, 512, 1, false>(),   xkernel<ff, 512, 2, false>(),   xkernel<ff, 512, 4, false>(),
+        xkernel<ff, 512, 8, false>(),   xkernel<ff, 1024, 8, false>(),  xkernel<ff, 1024, 16, false>(),
         xkernel<ff, 2048, 16, false>(), xkernel<ff, 4096, 16, false>(),
     };
     return v;

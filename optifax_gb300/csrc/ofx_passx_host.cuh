@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "ofx_desc.cuh"
@@ -44,9 +45,15 @@ __global__ void passx_twiddles(typename Num<R>::cplx* out, int n) {
 }
 
 // points per CTA: clusters of up to 16 CTAs, at most 1024 points per CTA below
-// 2^15 points (the FP64 rate bounds this kernel, so more SMs per pulse pay)
+// 2^15 points (the FP64 rate bounds this kernel, so more SMs per pulse pay).
+// Float-float spreads further up to 2^12 points, 512 per CTA (GB300, 0.3 mm pass:
+// 2^11 13.6 against 18.6 us per attempt, 2^12 16.3 against 19.3); at 2^13, 16 CTAs
+// of 512 points lose to 8 of 1024 (26.6 against 21.7 us), and 2048 or 4096 points
+// per CTA lose at every size (2^14: 50.1 and 90.6 against 38.6 us).
+template <typename R>
 inline int passx_cta_points(int n) {
     int m = n < 1024 ? n : 1024;
+    if (std::is_same<R, ff>::value && n <= 4096) m = n < 512 ? n : 512;
     if (n / m > 16) m = n / 16;
     return m;
 }
@@ -90,7 +97,7 @@ int passx_run(const std::vector<XKernel<R>>& kernels, XWork<R>& w, int n, int B,
     if (64LL * (S + 16) + 64 > 0x7fffffffLL) return OPTIFAX_ERR_INVALID_ARGUMENT;
     VariantCfg vc;
     if (variant == OPTIFAX_VARIANT_ODE23 || !variant_cfg(variant, &vc)) return OPTIFAX_ERR_INVALID_ARGUMENT;
-    const int M = passx_cta_points(n), C = n / M;
+    const int M = passx_cta_points<R>(n), C = n / M;
     const XKernel<R>* ke = nullptr;
     for (const auto& k : kernels)
         if (k.M == M && k.C == C && k.nee == (vc.nee != 0)) ke = &k;
