@@ -528,6 +528,62 @@ def gnlse_cpu_sample(T, w0, betas, A, length, gpu_attempts, fraction=0.1):
                       f"{el1:.1f} s): {v_one:.4f} propagations/s"}
 
 
+def run_fastforward(args):
+    """Config 5 at its own size: the surrogate+solver loop over --ff-trips round trips
+    (default 1000) of the 2^14-point SPOPO, a solver check every 10 trips on the
+    fed-back band's energy (5 %), the solver finishing the last 50, from the cavity
+    after --warmup solver trips; beside it the solver alone over the same trips from
+    the same state and the persistent FP64 kernel over two trips.  value = the
+    loop's round trips per second (wall clock, the checks and hand-overs included)."""
+    import numpy as np
+    import torch
+    from optifax_gb300 import opo, fastforward as ff
+    from optifax_gb300.surrogate import FNO, pretrained
+    spec = _spec()
+    dev = torch.device("cuda:0")
+    warm = opo.OpticalSim(spec)
+    warm.run(args.warmup)
+    start = warm.field.clone()
+    params, meta = pretrained()
+    crop = ff.reference_env_crop(spec)
+    net = FNO(n_bins=crop.n_bins, max_batch=1, params=params)
+    runs = {}
+    with ClockSampler(0) as clk:
+        for name, model in (("surrogate", net), ("solver", None)):
+            s_ = opo.OpticalSim(spec)
+            s_.field = start.clone()
+            runs[name] = ff.run_fast_forward(s_, model, crop, max_trips=args.ff_trips, check_every=10,
+                                             check_tol=0.05, finish_trips=50, check="energy")
+    fr, fo = runs["surrogate"], runs["solver"]
+    fp64 = ff.fp64_plain_trips(spec, 2, device=0, E0=start.cpu().numpy().astype(np.complex128))
+    e_s, e_o = np.array(fr["energies"]), np.array(fo["energies"])
+    fbm = np.abs(s_.feedback.cpu().numpy()) > 0
+    final = ff.phase_aligned_err(np.fft.fft(fr["field"].cpu().numpy()), np.fft.fft(fo["field"].cpu().numpy()), fbm)
+    ce = np.array(fr["check_energy_err"])
+    line = {"metric": "OPO round-trips/s surrogate+solver (config 5: 1000 trips, check every 10)",
+            "value": fr["trips_per_s"], "unit": UNIT, "n_gpus": 1, "steps": fr["trips"], "warmup": args.warmup,
+            "ms_per_step": 1000.0 * fr["wall_s"] / max(fr["trips"], 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD + f"; {args.ff_trips} trips from the cavity after {args.warmup} "
+                                              "solver trips", "check": "fed-back band energy within 5 %, every "
+                                              "10 trips; the solver runs the last 50",
+                       "network": f"FNO trained on {meta['pairs']} solver pairs (shipped weights)"},
+            "surrogate_trips": fr["surrogate_trips"], "solver_trips": fr["solver_trips"],
+            "checks": int(len(ce)), "checks_passed": int(np.sum(ce <= 0.05)),
+            "check_energy_err_median": float(np.median(ce)) if len(ce) else None,
+            "check_field_err_median": float(np.median(fr["check_field_err"])) if len(ce) else None,
+            "solver_only": {"trips": fo["trips"], "trips_per_s": fo["trips_per_s"], "wall_s": fo["wall_s"]},
+            "speedup_over_solver_only": fr["trips_per_s"] / fo["trips_per_s"],
+            "fp64_plain_trips_per_s": fp64["trips_per_s"],
+            "speedup_over_fp64": fr["trips_per_s"] / fp64["trips_per_s"],
+            "output_signal_energy_j": {"surrogate_loop": {"mean": float(e_s.mean()), "std": float(e_s.std())},
+                                       "solver_only": {"mean": float(e_o.mean()), "std": float(e_o.std())}},
+            "mean_energy_rel_diff": float(abs(e_s.mean() - e_o.mean()) / max(abs(e_o.mean()), 1e-300)),
+            "final_input_rel_l2_vs_solver_only": final,
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
 def run_gnlse(args):
     """chi(3) fibre (gnlsefib.m) power scan: 152 pulses (one per SM), 4096 points over
     6 ps, sech pulses of 28.4 fs at 835 nm with 1-10 kW peak power, 15 cm of fibre
@@ -677,9 +733,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cta-points", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="opo", choices=["opo", "sweep", "gnlse"],
+    ap.add_argument("--workload", default="opo", choices=["opo", "sweep", "gnlse", "fastforward"],
                     help="opo: 2^14-point SPOPO round trips (default line); sweep: 256 uneven batched passes; "
-                         "gnlse: chi(3) fibre power scan (152 pulses)")
+                         "gnlse: chi(3) fibre power scan (152 pulses); fastforward: the surrogate+solver loop "
+                         "over --ff-trips trips beside the solver alone (config 5)")
+    ap.add_argument("--ff-trips", type=int, default=1000)
     ap.add_argument("--sweep-size", type=int, default=256)
     ap.add_argument("--fp64-trips", type=int, default=2,
                     help="round trips of the plain FP64 solver timed beside the line, from the timed window's "
@@ -711,6 +769,8 @@ def main():
         return run_sweep(args)
     if args.workload == "gnlse":
         return run_gnlse(args)
+    if args.workload == "fastforward":
+        return run_fastforward(args)
 
     import numpy as np
     import torch
