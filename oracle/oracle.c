@@ -40,12 +40,13 @@
  * Threads: independent schedules (pulses) run in parallel.  A call with one
  * schedule of 4096 points or more and an explicit thread count (nthreads > 1)
  * spreads the pass over those threads instead; with nthreads = 0 a pass stays
- * on one thread.  The Heun MEX schedule of one pulse runs as one parallel
- * region per pass (run_heun_mex_team): each thread owns a span of points, updates
- * both stages of its span with a two-point halo, and runs the FFT stages that fit
- * its span without synchronisation, so a rejected attempt costs one barrier and
- * an accepted one 2 log2(T) + 4.  The other schedules spread each point loop and
- * FFT stage separately.  Each point's arithmetic is the same whichever thread
+ * on one thread.  The Heun MEX and RK23 schedules of one pulse run as one
+ * parallel region per pass (run_heun_mex_team, run_rk23_mex_team): each thread
+ * owns a span of points, updates the stages of its span with a halo of two (Heun)
+ * or three (RK23) points, and runs the FFT stages that fit its span without
+ * synchronisation, so a rejected Heun attempt costs one barrier and an accepted
+ * one 2 log2(T) + 4.  The NEE schedule spreads each point loop and FFT stage
+ * separately.  Each point's arithmetic is the same whichever thread
  * does it and the only reductions (a max and an OR) are exact, so the results do
  * not depend on the thread count.
  */
@@ -388,6 +389,42 @@ static int team_size(int n, int nb) {
     return t;
 }
 
+/* dispersion_step for the points [tid n/T, (tid+1) n/T) of one pulse, called by
+ * every thread of a team after the barrier that completes E: the absorber is
+ * applied in the bit-reversal gather into y (a free n-point buffer), the dispersion
+ * factor (this thread's points of the cached table for step size s; my_s is the
+ * thread's view of the cache slots) in the gather back into E, then A0 = E / N on
+ * the thread's points.  Thread 0 records stepmods[kidx].  Ends without a barrier:
+ * the caller adds one after any further writes of its own points. */
+static void dispersion_team(sched_ctx* c, work* w, cplx* y, double* my_s, int s, int chunk, int nchunks,
+                            int kidx, int tid, int T) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N, span = n / T, lo = tid * span, hi = lo + span;
+    const double inv_n = 1.0 / (double)n;
+    const int slot = disp_slot((double)s);
+    cplx* f = w->disp + (size_t)slot * (size_t)n;
+    if (my_s[slot] != (double)s) {
+        for (int i = lo; i < hi; ++i)
+            f[i] = cscale(cexpi(-c->beta[i] * (double)s), pow(c->alpha[i], (double)s));
+        my_s[slot] = (double)s;
+    }
+    const int* rev = w->plan.rev;
+    cplx* e = w->E;
+    for (int i = lo; i < hi; ++i) y[i] = cscale(e[rev[i]], w->abc[rev[i]]);
+    fft_team_stages(&w->plan, y, 0, tid, T);
+    if (c->Ap) {
+        long long off = ((long long)c->b0 * nchunks + chunk) * (long long)n;
+        if (off >= 0 && off + n <= c->ap_len) {
+            for (int i = lo; i < hi; ++i) c->Ap[off + i] = cmul(y[i], f[i]);
+        } else if (tid == 0) c->stats->status |= OFX_ORACLE_STATUS_AP_RANGE;
+    }
+    for (int i = lo; i < hi; ++i) e[i] = cmul(y[rev[i]], f[rev[i]]);
+    fft_team_stages(&w->plan, e, 1, tid, T);
+    for (int i = lo; i < hi; ++i) w->A0[i] = cscale(e[i], inv_n);
+    if (tid == 0 && c->stepmods && kidx < p->stepmods_limit && kidx < p->S && kidx >= 0)
+        c->stepmods[kidx] = (double)s;
+}
+
 /* Both Heun stages and the error test for points [lo, hi) of one pulse.  The
  * centred difference in K needs NL one point further out on each side, and the
  * second stage needs A1 (hence K1) one point further out again, so the span
@@ -433,7 +470,7 @@ static int heun_span(const ofx_oracle_params* p, const cplx* A0, cplx* E, const 
 static int run_heun_mex_team(sched_ctx* c, work* w, int T) {
     const ofx_oracle_params* p = c->p;
     const int n = p->N, span = n / T;
-    const double sel = p->sel, inv_n = 1.0 / (double)n, c_shock = 1.0 / (2.0 * p->dt * p->w0);
+    const double sel = p->sel, c_shock = 1.0 / (2.0 * p->dt * p->w0);
     int nchunks = (int)((double)p->S / sel);
     if (p->chunk_mode == OFX_CHUNKS_CEIL && (double)nchunks * sel < (double)p->S) nchunks += 1;
     cplx* scratch = (cplx*)malloc(sizeof(cplx) * 4 * (size_t)(span + 4) * (size_t)T);
@@ -486,31 +523,7 @@ static int run_heun_mex_team(sched_ctx* c, work* w, int T) {
                             c->stats->accepted++;
                             c->stats->z_steps += (long long)stepmod;
                         }
-                        /* dispersion_step on this thread's points: the absorber is
-                         * applied in the bit-reversal gather into K1 (free in this
-                         * path), the dispersion factor in the gather back into E */
-                        const int slot = disp_slot((double)s);
-                        cplx* f = w->disp + (size_t)slot * (size_t)n;
-                        if (my_s[slot] != (double)s) {
-                            for (int i = lo; i < hi; ++i)
-                                f[i] = cscale(cexpi(-c->beta[i] * (double)s), pow(c->alpha[i], (double)s));
-                            my_s[slot] = (double)s;
-                        }
-                        const int* rev = w->plan.rev;
-                        cplx *e = w->E, *y = w->K1;
-                        for (int i = lo; i < hi; ++i) y[i] = cscale(e[rev[i]], w->abc[rev[i]]);
-                        fft_team_stages(&w->plan, y, 0, tid, T);
-                        if (c->Ap) {
-                            long long off = ((long long)c->b0 * nchunks + chunk) * (long long)n;
-                            if (off >= 0 && off + n <= c->ap_len) {
-                                for (int i = lo; i < hi; ++i) c->Ap[off + i] = cmul(y[i], f[i]);
-                            } else if (tid == 0) c->stats->status |= OFX_ORACLE_STATUS_AP_RANGE;
-                        }
-                        for (int i = lo; i < hi; ++i) e[i] = cmul(y[rev[i]], f[rev[i]]);
-                        fft_team_stages(&w->plan, e, 1, tid, T);
-                        for (int i = lo; i < hi; ++i) w->A0[i] = cscale(e[i], inv_n);
-                        if (tid == 0 && c->stepmods && kidx < p->stepmods_limit && kidx < p->S && kidx >= 0)
-                            c->stepmods[kidx] = (double)s;
+                        dispersion_team(c, w, w->K1, my_s, s, chunk, nchunks, kidx, tid, T);
 #pragma omp barrier
                         if (k + stepmod >= cend && k < cend - 1.0) {
                             stepend = (cend - k) - 1.0;
@@ -519,6 +532,172 @@ static int run_heun_mex_team(sched_ctx* c, work* w, int T) {
                         } else {
                             if (!(fl & 2) && !(fl & 1) && (k + stepmod + 1.0) < cend - 1.0)
                                 stepmod = stepmod + 1.0;
+                            stepprev = stepmod;
+                        }
+                    }
+                    attempt++;
+                }
+            }
+            if (tid == 0) {
+                c->stats->attempts = attempt;
+                c->stats->k_final = k;
+                c->stats->stepmod_final = stepmod;
+                c->stats->nchunks = nchunks;
+                if (c->n_attempts) *c->n_attempts = attempt;
+                ran = 1;
+            }
+        }
+    }
+    free(scratch); free(part_pm); free(part_fl);
+    return ran ? 0 : -1;
+}
+
+/* The three Bogacki-Shampine stages after K1 and the error test for points
+ * [lo, hi) of one pulse (run_rk23_mex's attempt).  K4 at a point needs the drive
+ * of E one point out, E needs K3 there, K3 the drive of A1' = A0 + 3/4 K2 two
+ * points out and K2 the drive of A1 three points out, so the span recomputes
+ * NL2, K2 and A1' on [lo-3, hi+3) and [lo-2, hi+2), K3 and E on [lo-1, hi+1)
+ * (indices periodic), reading A0, A1 and K1 of the whole pulse.  Every value is
+ * the expression run_rk23_mex evaluates for that point.  Writes E and K4 on
+ * [lo, hi); the new A1 is only classified.  Scratch: 6 (hi - lo + 6) values. */
+static int rk23_span(const ofx_oracle_params* p, const cplx* A0, const cplx* A1, const cplx* K1, cplx* E, cplx* K4,
+                     const cplx* cw0, int lo, int hi, cplx ez2, cplx ez3, cplx ez4, double hmod, double g,
+                     double c_shock, cplx* scratch, double* pm) {
+    const int n = p->N, m = hi - lo + 6;
+    cplx *nl2 = scratch, *k2 = scratch + m, *nl3 = scratch + 2 * m, *k3 = scratch + 3 * m;
+    cplx *ev = scratch + 4 * m, *nl4 = scratch + 5 * m;
+#define OFX_WRAP(i) ((i) < 0 ? (i) + n : ((i) >= n ? (i) - n : (i)))
+    for (int l = 0; l < m; ++l) {                       /* point lo - 3 + l */
+        const int gi = OFX_WRAP(lo - 3 + l);
+        nl2[l] = nl_point(A1[gi], cw0[gi], ez2);
+    }
+    for (int l = 1; l < m - 1; ++l) {
+        const int gi = OFX_WRAP(lo - 3 + l);
+        k2[l] = k_point(nl2[l + 1], nl2[l - 1], nl2[l], hmod, g, c_shock);
+        nl3[l] = nl_point(cadd(A0[gi], cscale(k2[l], 0.75)), cw0[gi], ez3);
+    }
+    for (int l = 2; l < m - 2; ++l) {
+        const int gi = OFX_WRAP(lo - 3 + l);
+        k3[l] = k_point(nl3[l + 1], nl3[l - 1], nl3[l], hmod, g, c_shock);
+        cplx e = cadd(A0[gi], cadd(cscale(k3[l], 4.0 / 9.0), cscale(k2[l], 1.0 / 3.0)));
+        ev[l] = cadd(e, cscale(K1[gi], 2.0 / 9.0));
+        nl4[l] = nl_point(ev[l], cw0[gi], ez4);
+    }
+#undef OFX_WRAP
+    int flags = 0;
+    for (int l = 3; l < m - 3; ++l) {
+        const int i = lo - 3 + l;
+        cplx k4 = k_point(nl4[l + 1], nl4[l - 1], nl4[l], hmod, g, c_shock);
+        cplx a = cadd(A0[i], cadd(cscale(k4, 1.0 / 8.0), cscale(k3[l], 1.0 / 3.0)));
+        a = cadd(a, cscale(k2[l], 1.0 / 4.0));
+        a = cadd(a, cscale(K1[i], 7.0 / 24.0));
+        E[i] = ev[l];
+        K4[i] = k4;
+        flags |= classify_point(p, ev[l], a, 200.0, pm);
+    }
+    return flags;
+}
+
+/* K1 = f(A0) at z = pos with the drive's G value g, and A1 = A0 + K1 / 2, on
+ * [lo, hi) (NL recomputed one point out on each side). */
+static void rk23_k1_span(const ofx_oracle_params* p, const cplx* A0, cplx* K1, cplx* A1, const cplx* cw0, int lo,
+                         int hi, cplx ez, double hmod, double g, double c_shock, cplx* scratch) {
+    const int n = p->N, m = hi - lo + 2;
+    cplx* nl = scratch;
+    for (int l = 0; l < m; ++l) {
+        int gi = lo - 1 + l;
+        gi = gi < 0 ? gi + n : (gi >= n ? gi - n : gi);
+        nl[l] = nl_point(A0[gi], cw0[gi], ez);
+    }
+    for (int l = 1; l < m - 1; ++l) {
+        const int i = lo - 1 + l;
+        K1[i] = k_point(nl[l + 1], nl[l - 1], nl[l], hmod, g, c_shock);
+        A1[i] = cadd(A0[i], cscale(K1[i], 0.5));
+    }
+}
+
+/* run_rk23_mex for one pulse on a team of T threads (as run_heun_mex_team): the
+ * stages on each thread's span, one barrier for the error test, K1 (FSAL: the
+ * accepted attempt's K4) and A1 = A0 + K1/2 kept for the whole pulse between
+ * attempts.  Bit-identical to run_rk23_mex.  Returns 0, or -1 (nothing done). */
+static int run_rk23_mex_team(sched_ctx* c, work* w, int T) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N, span = n / T;
+    const double sel = p->sel, c_shock = 1.0 / (2.0 * p->dt * p->w0);
+    int nchunks = (int)((double)p->S / sel);
+    if (p->chunk_mode == OFX_CHUNKS_CEIL && (double)nchunks * sel < (double)p->S) nchunks += 1;
+    cplx* scratch = (cplx*)malloc(sizeof(cplx) * 6 * (size_t)(span + 6) * (size_t)T);
+    double* part_pm = (double*)malloc(sizeof(double) * 2 * (size_t)T);
+    int* part_fl = (int*)malloc(sizeof(int) * 2 * (size_t)T);
+    int ran = 0;
+    if (scratch && part_pm && part_fl) {
+#pragma omp parallel num_threads(T)
+        if (omp_get_num_threads() == T) {
+            const int tid = omp_get_thread_num(), lo = tid * span, hi = lo + span;
+            cplx* mine = scratch + 6 * (size_t)(span + 6) * (size_t)tid;
+            cplx *K1 = w->K1, *K4 = w->K4;
+            double k = 0.0, stepprev = 4.0, stepmod = stepprev, stepend, pm = 0.0;
+            double my_s[OFX_DISP_SLOTS];
+            for (int j = 0; j < OFX_DISP_SLOTS; ++j) my_s[j] = -1.0;
+            int attempt = 0;
+            /* initial K1 at k = 0 (:432-438) */
+            rk23_k1_span(p, w->A0, K1, w->A1, w->cw0, lo, hi, cexpi(-(p->bdiffw0 * k * p->h)),
+                         stepmod * p->h, g_at(c, 0, 0), c_shock, mine);
+#pragma omp barrier
+            for (int chunk = 0; chunk < nchunks; ++chunk) {
+                stepmod = stepprev;
+                double cend = (double)(chunk + 1) * sel;
+                for (; k < cend && (p->chunk_mode != OFX_CHUNKS_CEIL || k < (double)p->S); k = k + stepmod) {
+                    const int kidx = (int)k;
+                    const double hmod = stepmod * p->h, g = g_at(c, kidx, 0);
+                    const cplx ez2 = cexpi(-(p->bdiffw0 * (k + 0.5 * stepmod) * p->h));
+                    const cplx ez3 = cexpi(-(p->bdiffw0 * (k + 0.75 * stepmod) * p->h));
+                    const cplx ez4 = cexpi(-(p->bdiffw0 * (k + stepmod) * p->h));
+                    double my_pm = 0.0;
+                    const int slot = attempt & 1;
+                    part_fl[slot * T + tid] = rk23_span(p, w->A0, w->A1, K1, w->E, K4, w->cw0, lo, hi, ez2, ez3,
+                                                        ez4, hmod, g, c_shock, mine, &my_pm);
+                    part_pm[slot * T + tid] = my_pm;
+#pragma omp barrier
+                    int fl = 0;
+                    pm = 0.0;
+                    for (int t = 0; t < T; ++t) {
+                        fl |= part_fl[slot * T + t];
+                        if (part_pm[slot * T + t] > pm) pm = part_pm[slot * T + t];
+                    }
+                    fl = get_flags(c, attempt, fl);
+                    if (tid == 0) {
+                        if (fl & 4) c->stats->status |= OFX_ORACLE_STATUS_NAN;
+                        c->stats->pct_max_last = pm;
+                    }
+                    if ((fl & 1) && stepmod > 1.0 && (k - stepmod) > 0.0) {
+                        if (tid == 0) { record(c, attempt, kidx, (int)stepmod, fl, 0); c->stats->rejected++; }
+                        k = k - stepmod;
+                        stepmod = stepmod - 1.0;
+                        stepprev = stepmod;
+                        /* K1 recomputed at the new start, G index k (:484-487) */
+                        rk23_k1_span(p, w->A0, K1, w->A1, w->cw0, lo, hi,
+                                     cexpi(-(p->bdiffw0 * (k + stepmod) * p->h)), stepmod * p->h,
+                                     g_at(c, (int)k, 0), c_shock, mine);
+#pragma omp barrier
+                    } else {
+                        const int s = (int)stepmod;
+                        if (tid == 0) {
+                            record(c, attempt, kidx, s, fl, 1);
+                            c->stats->accepted++;
+                            c->stats->z_steps += (long long)stepmod;
+                        }
+                        dispersion_team(c, w, w->K3, my_s, s, chunk, nchunks, kidx, tid, T);
+                        cplx* tk = K1; K1 = K4; K4 = tk;     /* FSAL swap (:512-514) */
+                        for (int i = lo; i < hi; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
+#pragma omp barrier
+                        if (k + stepmod >= cend && k < cend - 1.0) {
+                            stepend = (cend - k) - 1.0;
+                            stepprev = stepmod;
+                            stepmod = stepend;
+                        } else {
+                            if (!(fl & 2) && !(fl & 1) && (k + stepmod + stepmod) < cend - 1.0)
+                                stepmod = stepmod * 2.0;
                             stepprev = stepmod;
                         }
                     }
@@ -718,7 +897,14 @@ static int run_schedule(sched_ctx* c) {
 #else
         run_heun_mex(c, &w);
 #endif
-    } else if (p->method == OFX_ORACLE_RK23_MEX) run_rk23_mex(c, &w);
+    } else if (p->method == OFX_ORACLE_RK23_MEX) {
+#ifdef _OPENMP
+        int T = team_size(p->N, c->nb);
+        if (T < 2 || run_rk23_mex_team(c, &w, T) != 0) run_rk23_mex(c, &w);
+#else
+        run_rk23_mex(c, &w);
+#endif
+    }
     else run_heun_nee(c, &w);
     memcpy(c->A_out + (size_t)c->b0 * p->N, w.A0, sizeof(cplx) * (size_t)p->N * c->nb);
     work_free(&w);
