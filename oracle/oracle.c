@@ -40,13 +40,13 @@
  * Threads: independent schedules (pulses) run in parallel.  A call with one
  * schedule of 4096 points or more and an explicit thread count (nthreads > 1)
  * spreads the pass over those threads instead; with nthreads = 0 a pass stays
- * on one thread.  The Heun MEX and RK23 schedules of one pulse run as one
- * parallel region per pass (run_heun_mex_team, run_rk23_mex_team): each thread
+ * on one thread.  Each schedule of one pulse runs as one parallel region per
+ * pass (run_heun_mex_team, run_rk23_mex_team, run_heun_nee_team): each thread
  * owns a span of points, updates the stages of its span with a halo of two (Heun)
  * or three (RK23) points, and runs the FFT stages that fit its span without
  * synchronisation, so a rejected Heun attempt costs one barrier and an accepted
- * one 2 log2(T) + 4.  The NEE schedule spreads each point loop and FFT stage
- * separately.  Each point's arithmetic is the same whichever thread
+ * one 2 log2(T) + 4.  A batch sharing one schedule spreads each point loop and
+ * FFT stage separately instead.  Each point's arithmetic is the same whichever thread
  * does it and the only reductions (a max and an OR) are exact, so the results do
  * not depend on the thread count.
  */
@@ -394,10 +394,11 @@ static int team_size(int n, int nb) {
  * applied in the bit-reversal gather into y (a free n-point buffer), the dispersion
  * factor (this thread's points of the cached table for step size s; my_s is the
  * thread's view of the cache slots) in the gather back into E, then A0 = E / N on
- * the thread's points.  Thread 0 records stepmods[kidx].  Ends without a barrier:
- * the caller adds one after any further writes of its own points. */
+ * the thread's points.  With records (the MEX schedules) the spectrum is also
+ * snapshotted into Ap and thread 0 records stepmods[kidx].  Ends without a
+ * barrier: the caller adds one after any further writes of its own points. */
 static void dispersion_team(sched_ctx* c, work* w, cplx* y, double* my_s, int s, int chunk, int nchunks,
-                            int kidx, int tid, int T) {
+                            int kidx, int tid, int T, int records) {
     const ofx_oracle_params* p = c->p;
     const int n = p->N, span = n / T, lo = tid * span, hi = lo + span;
     const double inv_n = 1.0 / (double)n;
@@ -412,7 +413,7 @@ static void dispersion_team(sched_ctx* c, work* w, cplx* y, double* my_s, int s,
     cplx* e = w->E;
     for (int i = lo; i < hi; ++i) y[i] = cscale(e[rev[i]], w->abc[rev[i]]);
     fft_team_stages(&w->plan, y, 0, tid, T);
-    if (c->Ap) {
+    if (records && c->Ap) {
         long long off = ((long long)c->b0 * nchunks + chunk) * (long long)n;
         if (off >= 0 && off + n <= c->ap_len) {
             for (int i = lo; i < hi; ++i) c->Ap[off + i] = cmul(y[i], f[i]);
@@ -421,7 +422,7 @@ static void dispersion_team(sched_ctx* c, work* w, cplx* y, double* my_s, int s,
     for (int i = lo; i < hi; ++i) e[i] = cmul(y[rev[i]], f[rev[i]]);
     fft_team_stages(&w->plan, e, 1, tid, T);
     for (int i = lo; i < hi; ++i) w->A0[i] = cscale(e[i], inv_n);
-    if (tid == 0 && c->stepmods && kidx < p->stepmods_limit && kidx < p->S && kidx >= 0)
+    if (records && tid == 0 && c->stepmods && kidx < p->stepmods_limit && kidx < p->S && kidx >= 0)
         c->stepmods[kidx] = (double)s;
 }
 
@@ -523,7 +524,7 @@ static int run_heun_mex_team(sched_ctx* c, work* w, int T) {
                             c->stats->accepted++;
                             c->stats->z_steps += (long long)stepmod;
                         }
-                        dispersion_team(c, w, w->K1, my_s, s, chunk, nchunks, kidx, tid, T);
+                        dispersion_team(c, w, w->K1, my_s, s, chunk, nchunks, kidx, tid, T, 1);
 #pragma omp barrier
                         if (k + stepmod >= cend && k < cend - 1.0) {
                             stepend = (cend - k) - 1.0;
@@ -687,7 +688,7 @@ static int run_rk23_mex_team(sched_ctx* c, work* w, int T) {
                             c->stats->accepted++;
                             c->stats->z_steps += (long long)stepmod;
                         }
-                        dispersion_team(c, w, w->K3, my_s, s, chunk, nchunks, kidx, tid, T);
+                        dispersion_team(c, w, w->K3, my_s, s, chunk, nchunks, kidx, tid, T, 1);
                         cplx* tk = K1; K1 = K4; K4 = tk;     /* FSAL swap (:512-514) */
                         for (int i = lo; i < hi; ++i) w->A1[i] = cadd(w->A0[i], cscale(K1[i], 0.5));
 #pragma omp barrier
@@ -702,6 +703,127 @@ static int run_rk23_mex_team(sched_ctx* c, work* w, int T) {
                         }
                     }
                     attempt++;
+                }
+            }
+            if (tid == 0) {
+                c->stats->attempts = attempt;
+                c->stats->k_final = k;
+                c->stats->stepmod_final = stepmod;
+                c->stats->nchunks = nchunks;
+                if (c->n_attempts) *c->n_attempts = attempt;
+                ran = 1;
+            }
+        }
+    }
+    free(scratch); free(part_pm); free(part_fl);
+    return ran ? 0 : -1;
+}
+
+/* Both stages of NEE_CPU.m's Heun step and its error measure for points [lo, hi)
+ * (halo as heun_span): A1 = A0 + K1, E = (A0 + K1/2) + K2/2, the largest
+ * 100 |E - A1| / (|E| + 1) into *pm, and *nan set when A0 holds a NaN on these
+ * points (the schedule tests A0 before the step; the caller discards the step
+ * then).  Writes E on [lo, hi).  Scratch: 4 (hi - lo + 4) values. */
+static void nee_span(const ofx_oracle_params* p, const cplx* A0, cplx* E, const cplx* cw0, int lo, int hi,
+                     cplx ez1, cplx ez2, double hmod, double g, double c_shock, cplx* scratch, double* pm, int* nan) {
+    const int n = p->N, m = hi - lo + 4;
+    cplx *nl1 = scratch, *k1 = scratch + m, *a1 = scratch + 2 * m, *nl2 = scratch + 3 * m;
+#define OFX_WRAP(i) ((i) < 0 ? (i) + n : ((i) >= n ? (i) - n : (i)))
+    for (int l = 0; l < m; ++l) {
+        const int gi = OFX_WRAP(lo - 2 + l);
+        nl1[l] = nl_point(A0[gi], cw0[gi], ez1);
+    }
+    for (int l = 1; l < m - 1; ++l) {
+        const int gi = OFX_WRAP(lo - 2 + l);
+        k1[l] = k_point(nl1[l + 1], nl1[l - 1], nl1[l], hmod, g, c_shock);
+        a1[l] = cadd(A0[gi], k1[l]);
+        nl2[l] = nl_point(a1[l], cw0[gi], ez2);
+    }
+#undef OFX_WRAP
+    for (int l = 2; l < m - 2; ++l) {
+        const int i = lo - 2 + l;
+        if (isnan(A0[i].re) || isnan(A0[i].im)) *nan = 1;
+        cplx k2 = k_point(nl2[l + 1], nl2[l - 1], nl2[l], hmod, g, c_shock);
+        cplx e = cadd(cadd(A0[i], cscale(k1[l], 0.5)), cscale(k2, 0.5));
+        E[i] = e;
+        double v = 100.0 * cabs2(csub(e, a1[l])) / (cabs2(e) + 1.0);
+        if (v > *pm) *pm = v;
+    }
+}
+
+/* run_heun_nee for one pulse on a team of T threads (as run_heun_mex_team), with
+ * the chunk-end snapshot ApFT(:, chunk) = fft(A0) taken by the team too.
+ * Bit-identical to run_heun_nee.  Returns 0, or -1 (nothing done). */
+static int run_heun_nee_team(sched_ctx* c, work* w, int T) {
+    const ofx_oracle_params* p = c->p;
+    const int n = p->N, span = n / T;
+    const double c_shock = 1.0 / (2.0 * p->dt * p->w0);
+    const int nchunks = (int)floor((double)p->S / p->sel);
+    cplx* scratch = (cplx*)malloc(sizeof(cplx) * 4 * (size_t)(span + 4) * (size_t)T);
+    double* part_pm = (double*)malloc(sizeof(double) * 2 * (size_t)T);
+    int* part_fl = (int*)malloc(sizeof(int) * 2 * (size_t)T);
+    int ran = 0;
+    if (scratch && part_pm && part_fl) {
+#pragma omp parallel num_threads(T)
+        if (omp_get_num_threads() == T) {
+            const int tid = omp_get_thread_num(), lo = tid * span, hi = lo + span;
+            cplx* mine = scratch + 4 * (size_t)(span + 4) * (size_t)tid;
+            double k = 1.0, stepmod = 4.0, pm = 0.0;
+            double my_s[OFX_DISP_SLOTS];
+            for (int j = 0; j < OFX_DISP_SLOTS; ++j) my_s[j] = -1.0;
+            int attempt = 0, ev = 0;
+            for (int chunk = 1; chunk <= nchunks; ++chunk) {
+                while (k < (double)chunk * p->sel && k <= (double)p->S) {
+                    const int kidx = (int)k - 1;                /* G33(k), 1-based */
+                    const double hmod = p->h * stepmod, g = g_at(c, kidx, 0);
+                    const cplx ez1 = cexpi(-(p->bdiffw0 * (k - 1.0) * p->h));
+                    const cplx ez2 = cexpi(-(p->bdiffw0 * (k - 1.0 + stepmod) * p->h));
+                    double my_pm = 0.0;
+                    int my_nan = 0;
+                    const int slot = ev & 1;
+                    nee_span(p, w->A0, w->E, w->cw0, lo, hi, ez1, ez2, hmod, g, c_shock, mine, &my_pm, &my_nan);
+                    part_fl[slot * T + tid] = my_nan;
+                    part_pm[slot * T + tid] = my_pm;
+                    ++ev;
+#pragma omp barrier
+                    int nan = 0;
+                    pm = 0.0;
+                    for (int t = 0; t < T; ++t) {
+                        nan |= part_fl[slot * T + t];
+                        if (part_pm[slot * T + t] > pm) pm = part_pm[slot * T + t];
+                    }
+                    if (nan) {
+                        if (tid == 0) c->stats->status |= OFX_ORACLE_STATUS_NAN;
+                        break;
+                    }
+                    int fl = (pm > p->maxErr ? 1 : 0) | (pm >= p->minErr ? 2 : 0);
+                    fl = get_flags(c, attempt, fl);
+                    if (tid == 0) c->stats->pct_max_last = pm;
+                    if ((fl & 1) && stepmod > 1.0) {
+                        if (tid == 0) { record(c, attempt, kidx + 1, (int)stepmod, fl, 0); c->stats->rejected++; }
+                        stepmod = stepmod - 1.0;
+                    } else {
+                        if (tid == 0) {
+                            record(c, attempt, kidx + 1, (int)stepmod, fl, 1);
+                            c->stats->accepted++;
+                            c->stats->z_steps += (long long)stepmod;
+                        }
+                        dispersion_team(c, w, w->K1, my_s, (int)stepmod, chunk - 1, nchunks, kidx, tid, T, 0);
+#pragma omp barrier
+                        if (!(fl & 2)) stepmod = stepmod + 1.0;     /* pcterr < minErr */
+                        if (k < (double)p->S && (k + stepmod) > (double)p->S) stepmod = (double)p->S - k;
+                        k = k + stepmod;
+                    }
+                    attempt++;
+                }
+                /* ApFT(:,chunk) = fft(Et) */
+                if (c->Ap) {
+                    long long off = ((long long)c->b0 * nchunks + (chunk - 1)) * (long long)n;
+                    if (off >= 0 && off + n <= c->ap_len) {
+                        cplx* ap = c->Ap + off;
+                        for (int i = lo; i < hi; ++i) ap[i] = w->A0[w->plan.rev[i]];
+                        fft_team_stages(&w->plan, ap, 0, tid, T);
+                    } else if (tid == 0) c->stats->status |= OFX_ORACLE_STATUS_AP_RANGE;
                 }
             }
             if (tid == 0) {
@@ -905,7 +1027,14 @@ static int run_schedule(sched_ctx* c) {
         run_rk23_mex(c, &w);
 #endif
     }
-    else run_heun_nee(c, &w);
+    else {
+#ifdef _OPENMP
+        int T = team_size(p->N, c->nb);
+        if (T < 2 || run_heun_nee_team(c, &w, T) != 0) run_heun_nee(c, &w);
+#else
+        run_heun_nee(c, &w);
+#endif
+    }
     memcpy(c->A_out + (size_t)c->b0 * p->N, w.A0, sizeof(cplx) * (size_t)p->N * c->nb);
     work_free(&w);
     return 0;

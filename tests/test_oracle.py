@@ -163,13 +163,14 @@ def test_undepleted_shg_follows_sinc(oracle):
     (4096, 2, "ABC_NONE", "HEUN_MEX"),
     (4096, 3, "ABC_SOFT", "RK23_MEX"),      # RK23 on a team of 2
     (8192, 8, "ABC_HARD", "RK23_MEX"),      # RK23 on 8 threads of 1024 points
-    (4096, 2, "ABC_NONE", "HEUN_NEE"),      # NEE: loop-by-loop threading
+    (4096, 2, "ABC_NONE", "HEUN_NEE"),      # NEE (its own absorber) on a team of 2
+    (8192, 8, "ABC_SOFT", "HEUN_NEE"),      # NEE on 8 threads, chunk-end snapshots by the team
 ])
 def test_threads_inside_one_pass_are_bit_identical(oracle, N, threads, abc, method):
     """A lone pass of 4096 points or more with an explicit thread count runs on a
-    team of threads (Heun and RK23: one parallel region per pass, each thread on its
-    own span; NEE: loop by loop); every result bit -- field, snapshots, stepmods,
-    trace, statistics -- is the same as on one thread."""
+    team of threads (one parallel region per pass, each thread on its own span of
+    points); every result bit -- field, snapshots, stepmods, trace, statistics --
+    is the same as on one thread."""
     win, si, E = make_case(N=N, length=0.03e-3, power=2.0)
     kw = dict(w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps, dt=si.dt, max_err=si.max_err,
               min_err=si.min_err, sel=si.sel, trace_cap=10000, abc_mode=getattr(oracle, abc),
@@ -183,7 +184,7 @@ def test_threads_inside_one_pass_are_bit_identical(oracle, N, threads, abc, meth
     assert one.stats == many.stats
 
 
-@pytest.mark.parametrize("method", ["HEUN_MEX", "RK23_MEX"])
+@pytest.mark.parametrize("method", ["HEUN_MEX", "RK23_MEX", "HEUN_NEE"])
 def test_threads_follow_forced_rejects(oracle, method):
     """Forced reject flags (which replay a GPU schedule) drive the threaded pass
     through the same rejected attempts as one thread."""
