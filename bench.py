@@ -125,7 +125,7 @@ def host_cores() -> int:
     return n
 
 
-def oracle_threads(spec, field=None, fraction=0.004):
+def oracle_threads(spec, field=None, fraction=0.02):
     """Threads for the single-cavity CPU baseline: one, a quarter, half or all of the
     host cores, whichever runs a short sample (the first `fraction` of the pass)
     fastest.  One pass is sequential in z; the oracle runs it as one parallel
