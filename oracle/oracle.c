@@ -13,7 +13,8 @@
  * cubins and driven with cuFFT by oracle/ref_mex.cpp.
  * tests/test_reference_kernels_gpu.py checks this restatement against them on
  * the GPU: identical step schedules (Heun), and fields within the drift of
- * cuFFT's FP32 round trips.  Known-answer tests
+ * cuFFT's FP32 round trips; tests/test_golden_cpu.py does the same on the CPU
+ * against their outputs saved in tests/golden/.  Known-answer tests
  * (pure dispersion, FFT, convergence order, replay, the reject rules) are in
  * tests/test_oracle.py.  The NEE_CPU.m schedule (MATLAB only) stays unpinned.
  *
