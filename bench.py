@@ -216,10 +216,12 @@ def cpu_replicas_sample(spec, field, attempts_per_trip, fraction=0.01, cores=Non
 
 def cpu_sweep_sample(insts, gpu_stats, cores, n_sample=16, fraction=0.02):
     """FP64 C oracle on a bounded sample of the sweep: the first `fraction` of the
-    steps of `n_sample` instances spread over the list.  Cost per unit of
-    attempts x N log2 N, measured on one core (serially) and on `cores` threads
-    (instances side by side; the oracle releases the GIL), scaled to the whole
-    sweep by the GPU's own attempt counts."""
+    steps of `n_sample` instances spread over the list, run one after another on one
+    core (the per-core rate, in attempts x N log2 N per second), and the parallel
+    efficiency of the host: one median-size sample instance alone against `cores`
+    copies of it side by side (the oracle releases the GIL).  The instances are
+    independent, so the aggregate CPU rate is cores x per-core rate x efficiency;
+    both figures are scaled to the whole sweep by the GPU's own attempt counts."""
     import concurrent.futures as cf
     import math
     import numpy as np
@@ -240,19 +242,28 @@ def cpu_sweep_sample(insts, gpu_stats, cores, n_sample=16, fraction=0.02):
         return r.stats[0]["attempts"] * n * math.log2(n)
 
     t0 = time.perf_counter()
-    work = sum(one(j) for j in jobs)
+    units = [one(j) for j in jobs]
     t_one = time.perf_counter() - t0
+    rate_1 = sum(units) / t_one
+    mid = jobs[int(np.argsort(units)[len(units) // 2])]
+    t0 = time.perf_counter()
+    one(mid)
+    t_alone = time.perf_counter() - t0
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=cores) as ex:
-        list(ex.map(one, jobs))
-    t_all = time.perf_counter() - t0
+        list(ex.map(one, [mid] * cores))
+    t_side = time.perf_counter() - t0
+    eff = min(1.0, t_alone / t_side)
     total = sum(st["attempts"] * i.n_points * math.log2(i.n_points) for st, i in zip(gpu_stats, insts))
-    est_one, est_all = t_one / work * total, t_all / work * total
+    est_one = total / rate_1
+    est_all = total / (cores * rate_1 * eff)
     return {"value": len(insts) / est_all, "unit": "passes/s", "cores": cores, "kind": "port",
-            "single_core": len(insts) / est_one,
+            "single_core": len(insts) / est_one, "parallel_efficiency": eff,
             "sample": f"FP64 C oracle, first {fraction:.0%} of the steps of {len(jobs)} of the {len(insts)} "
-                      f"instances ({t_one:.1f} s on 1 core, {t_all:.1f} s on {cores} threads), scaled to the "
-                      f"sweep by attempts x N log2 N with the GPU's attempt counts"}
+                      f"instances one after another on 1 core ({t_one:.1f} s), and one median instance alone "
+                      f"({t_alone:.2f} s) against {cores} copies side by side ({t_side:.2f} s): {cores} cores x "
+                      f"the per-core rate x {eff:.2f} efficiency, scaled to the sweep by attempts x N log2 N "
+                      f"with the GPU's attempt counts"}
 
 
 def reference_buildup(spec, trips=5):
@@ -922,7 +933,7 @@ def main():
 
     sweep_line = None
     if rank == 0 and world == 1 and not args.no_sweep:
-        sweep_line = sweep_record(1, 1, cpu_kw={"n_sample": 8, "fraction": 0.01})
+        sweep_line = sweep_record(1, 1, cpu_kw={"n_sample": 16, "fraction": 0.01})
 
     M = args.cta_points or min(N, 4096)
     if rank == 0:
