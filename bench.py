@@ -858,9 +858,12 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_oracle_sample(spec, fraction=0.05, field=timed_input,
+        # samples of ~10-20 s of CPU work: a fifth of a pass on the calibrated threads,
+        # and a twentieth of a pass on every core for the independent-cavity figure
+        cpu = cpu_oracle_sample(spec, fraction=0.2, field=timed_input,
                                 attempts_per_trip=attempts / K)
-        cpu["all_cores_independent_cavities"] = cpu_replicas_sample(spec, timed_input, attempts / K)
+        cpu["all_cores_independent_cavities"] = cpu_replicas_sample(spec, timed_input, attempts / K,
+                                                                    fraction=0.05)
 
     # the plain full-FP64 GPU solver (optifax_propagate_fp64, host cavity transfer in
     # FP64) on the same crystal input as the timed window: the metric's comparator,
