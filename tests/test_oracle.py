@@ -197,3 +197,21 @@ def test_threads_follow_forced_rejects(oracle, method):
     many = oracle.run(E, si.alpha, si.G, si.beta, nthreads=4, forced=forced, **kw)
     assert one.stats[0]["rejected"] >= 3
     assert np.array_equal(one.A, many.A) and np.array_equal(one.trace[0], many.trace[0])
+
+
+@pytest.mark.parametrize("method", ["HEUN_MEX", "RK23_MEX", "HEUN_NEE"])
+def test_threads_handle_a_nan_input_like_one_thread(oracle, method):
+    """A NaN in the input field: the MEX schedules flag it through the error test and
+    carry on, NEE_CPU's stops each chunk at its NaN test; the thread team does the
+    same as one thread, status and outputs alike."""
+    win, si, E = make_case(N=8192, length=0.01e-3, power=2.0)
+    E = E.copy()
+    E[0, 5000] = np.nan
+    kw = dict(w0=si.w0, bdiffw0=si.bdiffw0, h=si.h, n_steps=si.n_steps, dt=si.dt, max_err=si.max_err,
+              min_err=si.min_err, sel=si.sel, trace_cap=10000, method=getattr(oracle, method))
+    one = oracle.run(E, si.alpha, si.G, si.beta, nthreads=1, **kw)
+    many = oracle.run(E, si.alpha, si.G, si.beta, nthreads=4, **kw)
+    assert one.stats[0]["status"] & 1, one.stats[0]          # OFX_ORACLE_STATUS_NAN
+    assert one.stats == many.stats
+    assert np.array_equal(one.A, many.A, equal_nan=True)
+    assert np.array_equal(one.trace[0], many.trace[0])
